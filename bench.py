@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Benchmark: hex8 K+M(+F) assembly throughput on one GB300 (Melem/s).
+
+Workload (default): the 200x200x24-element seeded jittered steel block (1,010,025 nodes,
+960,000 elements, 26,367,673 3x3 blocks), FP64 K and M in BSR layout plus F with the
+centrifugal term for Omegas=(0,0,100), bottom face penalised.  A step is one pass of the
+path over that mesh: the element-integral kernel and the deterministic gather kernel.
+
+  value  : device-resident throughput (inputs already in HBM), CUDA events on the launch
+           stream, W warm-up steps then K timed steps, max over ranks.
+  e2e    : the same metric through the public Python API with host buffers: per step the
+           node coordinates are copied host->device from pinned memory, then
+           Model.Get_MatrixKL(), Get_MatrixM() and Get_VectorF() return scipy/numpy objects
+           (device->host copies included).
+  roofline: algorithmic bytes of one assembly (24N + 32E + 80 nnzb + 24N + 4 nnzb + 4(N+1))
+           / measured time, against the measured HBM copy bandwidth; the FP64 roofline of
+           the element kernel (analytic FP64 flops / time vs the measured FMA rate) is
+           reported beside it.
+  cpu_baseline / --impl reference: the C restatement of the reference algorithm (element
+           loop, per-element scratch, linear-search slot lookup, atomic scatter, penalty)
+           on all host cores.
+
+Multi-GPU (torchrun): every rank assembles its own replica of the workload (weak scaling,
+no data-path collective); value = all ranks' elements / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "K+M assembly Melem/s"
+UNIT = "Melem/s"
+
+# FP64 operations per element issued by k_hex8_element (counted from the kernel source):
+# phase A per Gauss point: J 72 FMA, adjugate 18, det 3, reciprocal ~10, R 72 (24x3),
+# R/det 24, load density ~40; phase B: 28 off-diagonal pairs x (72 + 4 + 21 + 1) +
+# 8 diagonal pairs x (48 + 8 + 14) + F 192.  Flops count an FMA as 2.
+ELEM_FP64_FLOPS = 2 * 8 * (72 + 72 + 24) + 8 * (18 + 3 + 10 + 40) + 28 * (2 * 76 + 21 + 1) + 8 * (2 * 56 + 14) + 2 * 192
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    return ap.parse_args()
+
+
+def algorithmic_bytes(N, E, nnzb):
+    """Minimum HBM bytes of one K+M+F assembly (coords, conn, K, M, F, pattern)."""
+    return 24 * N + 32 * E + 72 * nnzb + 8 * nnzb + 24 * N + 4 * nnzb + 4 * (N + 1)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def mesh_bc_arrays(P):
+    bn = np.concatenate([P.Nind[np.asarray(b[0])] for b in P.Bounds]) if P.Bounds else np.zeros(0, np.int64)
+    bc = np.zeros((bn.size, 3))
+    return bn, bc
+
+
+def cpu_sample_mesh(cfg):
+    """Bounded CPU sample of a workload: the same block family (element shape, jitter,
+    density, material, loads) with the x/y element counts halved until it has at most
+    240,000 elements."""
+    import fem_taichi_gb300 as F
+    kw = dict(F.CONFIGS[cfg])
+    while kw["nx"] * kw["ny"] * kw["nz"] > 240_000:
+        kw["nx"] //= 2
+        kw["ny"] //= 2
+        kw["size"] = (kw["size"][0] / 2, kw["size"][1] / 2, kw["size"][2])
+    return F.hex_block(name=cfg + "-sample", **kw)
+
+
+def run_cpu_port(P, mat, om, steps, warmup, threads):
+    """Times the C restatement of the reference algorithm (all threads); returns s/step."""
+    from oracle import c_oracle as C
+    bn, bc = mesh_bc_arrays(P)
+    nnzb = int(P.SmNode[-1])
+    out = (np.zeros((nnzb, 3, 3)), np.zeros(nnzb), np.zeros((P.Num_Node, 3)))
+    args = (P.xyz, P.conn, P.SmNode, P.ReNode, mat, om, bn, bc)
+    for _ in range(warmup):
+        C.assemble(*args, nthreads=threads, out=out)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        C.assemble(*args, nthreads=threads, out=out)
+    return (time.perf_counter() - t0) / max(steps, 1)
+
+
+def reference_arm(a):
+    ws, rank, _ = dist_setup("gloo")
+    if rank != 0:
+        return
+    import fem_taichi_gb300 as F
+    P = F.config_mesh(a.config)
+    S = cpu_sample_mesh(a.config)
+    thr = cpu_threads()
+    t = run_cpu_port(S, F.STEEL, (0, 0, 100), a.steps, a.warmup, thr)
+    v = S.Num_Elem / t / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(a.config, P), "threads": thr},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": f"{S.grid[0]}x{S.grid[1]}x{S.grid[2]} block of the {a.config} family "
+                                       f"({S.Num_Elem:,} elements, K+M+F) per step, {a.steps} steps"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": ("reference (Python/Taichi 0.6.28 + MKL Pardiso) cannot run on this image; timed: C restatement "
+                     "of its algorithm (oracle/fem_oracle.c) with OpenMP atomics on all host cores")}
+    print(json.dumps(line), flush=True)
+
+
+def workload_name(cfg, P):
+    return (f"{cfg}: hex8 K+M+F assembly, {P.grid[0]}x{P.grid[1]}x{P.grid[2]} elements ({P.Num_Node:,} nodes, "
+            f"{P.Num_Elem:,} elements, nnzb {int(P.SmNode[-1]):,}), FP64, BSR")
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return reference_arm(a)
+    import torch
+    ws, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import fem_taichi_gb300 as F
+    from fem_taichi_gb300 import _lib
+    from fem_taichi_gb300.model import _dptr, _stream
+    L = _lib.load()
+    mat, om = F.STEEL, (0, 0, 100)
+    t_mesh = time.perf_counter()
+    P = F.config_mesh(a.config)
+    t_mesh = time.perf_counter() - t_mesh
+    N, E, nnzb = P.Num_Node, P.Num_Elem, int(P.SmNode[-1])
+    model = F.Model(a.config, P, mat, Omegas=om, device=dev)
+    Kt = torch.empty((nnzb, 3, 3), dtype=torch.float64, device=dev)
+    Mt = torch.empty((nnzb,), dtype=torch.float64, device=dev)
+    Ft = torch.empty((N, 3), dtype=torch.float64, device=dev)
+    wsb = model.workspace()
+    out = _lib.FemAssemblyOut(_lib.LAYOUT_BSR, _lib.LAYOUT_BSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
+                              model.fixed.data_ptr(), model.loads.data_ptr())
+    st = _stream(dev)
+    stream = torch.cuda.current_stream(dev)
+    mesh_c, mat_c = ctypes.byref(model.mesh.c), ctypes.byref(model.mat)
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(L.fem_assemble_elements(mesh_c, mat_c, _dptr(wsb), wsb.numel(), st), "elements")
+        if ev is not None:
+            ev[1].record(stream)
+        _lib.check(L.fem_assemble_gather(mesh_c, ctypes.byref(out), _dptr(wsb), wsb.numel(), st), "gather")
+        if ev is not None:
+            ev[2].record(stream)
+
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(a.steps)]
+    clocks.start()
+    time.sleep(0.25)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(a.steps):
+        step(evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    el_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    ga_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_step = total_ms / a.steps
+    value = ws * E * a.steps / (total_ms * 1e-3) / 1e6
+
+    # -- roofline ---------------------------------------------------------------------------
+    peak, peak_kind = measured_peaks()
+    ab = algorithmic_bytes(N, E, nnzb)
+    achieved = ab / (ms_step * 1e-3) / 1e9
+    fp64_peak = ctypes.c_double(0)
+    _lib.check(L.fem_diag_fp64_tflops(ctypes.byref(fp64_peak), st), "fp64 probe")
+    fp64_ach = E * ELEM_FP64_FLOPS / (el_ms * 1e-3) / 1e12
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "assembly_c2_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("dram_bytes_per_assembly")
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded jittered hex block, steel, Omegas=(0,0,100))",
+            "config": {"workload": workload_name(a.config, P), "n_node": N, "n_elem": E, "nnzb": nnzb,
+                       "layout": "BSR K [nnzb][3][3], M [nnzb], F [N][3]",
+                       "l2": "inputs+outputs+workspace ~5.4 GB per step >> 129 MB L2 (no flush needed)",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "fem_assemble = k_hex8_element + k_gather (one assembly)",
+                         "algorithmic_bytes": ab,
+                         "fp64": {"kernel": "k_hex8_element", "achieved_tflops": fp64_ach,
+                                  "peak_tflops_measured": fp64_peak.value, "frac": fp64_ach / fp64_peak.value,
+                                  "flops_per_elem": ELEM_FP64_FLOPS}},
+            "kernels": {"k_hex8_element_ms": el_ms, "k_gather_ms": ga_ms,
+                        "share_element": el_ms / (el_ms + ga_ms), "share_gather": ga_ms / (el_ms + ga_ms)},
+            "gpu_launches": 2 * a.steps, "clocks": clk}
+
+    # -- e2e through the public API -------------------------------------------------------------
+    if not a.no_e2e:
+        ne = a.e2e_steps or max(3, min(a.steps, 10))
+        xyz_h = torch.from_numpy(P.xyz.copy()).pin_memory()
+
+        def e2e_step():
+            model.set_coordinates(xyz_h)
+            K = model.Get_MatrixKL()
+            M = model.Get_MatrixM()
+            Fv = model.Get_VectorF()
+            return K, M, Fv
+
+        for _ in range(2):
+            r = e2e_step()
+        del r
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(ne):
+            r = e2e_step()
+            del r
+        torch.cuda.synchronize()
+        w1 = time.perf_counter() - w0
+        if ws > 1:
+            tt = torch.tensor([w1], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            w1 = float(tt.item())
+        line["e2e"] = {"value": ws * E * ne / w1 / 1e6, "unit": UNIT, "h2d_bytes_per_step": 24 * N,
+                       "d2h_bytes_per_step": 72 * nnzb + 24 * nnzb + 24 * N, "steps": ne,
+                       "ms_per_step": w1 / ne * 1e3,
+                       "path": "Model.set_coordinates(pinned) + Get_MatrixKL + Get_MatrixM + Get_VectorF"}
+        line["e2e"]["gpu_launches"] = 2 * ne
+
+    # -- extras: stress recovery on the same mesh -------------------------------------------------
+    if not a.no_extras:
+        u = np.random.default_rng(2).uniform(-1e-3, 1e-3, size=(N, 3))
+        post = F.Post(a.config, P, mat, u, mesh=model.mesh)
+        Sout = torch.empty((N, 10), dtype=torch.float64, device=dev)
+        for _ in range(2):
+            post.stress_device(Sout)
+        torch.cuda.synchronize()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        ns = 5
+        s0.record(stream)
+        for _ in range(ns):
+            post.stress_device(Sout)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        sms = s0.elapsed_time(s1) / ns
+        sbytes = 24 * N + 24 * N + 32 * E + 80 * N + 4 * (N + 1) + 32 * E + 4 * N
+        line["stress"] = {"ms": sms, "algorithmic_bytes": sbytes, "gbs": sbytes / (sms * 1e-3) / 1e9,
+                          "frac_hbm": sbytes / (sms * 1e-3) / 1e9 / peak, "Mnodes_per_s": N / sms / 1e3}
+        line["stress"]["gpu_launches"] = 2 * ns
+        line["host_setup_s"] = {"mesh_and_pattern": t_mesh}
+
+    # -- CPU baseline (rank 0, N = 1) -----------------------------------------------------------
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        thr = cpu_threads()
+        S = cpu_sample_mesh(a.config)
+        ns = 8
+        t = run_cpu_port(S, mat, om, ns, 1, thr)
+        line["cpu_baseline"] = {"value": S.Num_Elem / t / 1e6, "unit": UNIT, "cores": thr, "kind": "port",
+                                "sample": f"{ns} assemblies (K+M+F) of the {S.grid[0]}x{S.grid[1]}x{S.grid[2]} "
+                                          f"block of the {a.config} family ({S.Num_Elem:,} elements) with "
+                                          f"oracle/fem_oracle.c on {thr} threads, {t:.2f} s each"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

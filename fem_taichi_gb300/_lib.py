@@ -1,0 +1,111 @@
+"""ctypes binding of ``libfemgb.so`` (the C ABI declared in ``include/fem_gb300.h``).
+
+The library is required: importing a GPU entry point without it raises.  There is no
+CPU fallback for any kernel.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+c_int64 = ctypes.c_int64
+c_int = ctypes.c_int
+c_double = ctypes.c_double
+c_void_p = ctypes.c_void_p
+c_size_t = ctypes.c_size_t
+
+FEM_OK = 0
+FEM_ERR_INVALID = -1
+FEM_ERR_CUDA = -2
+FEM_ERR_PATTERN = -3
+FEM_ERR_NOT_CONVERGED = -4
+FEM_ERR_MAXITER = -5
+FEM_ERR_NOT_SPD = -6
+FEM_ERR_WORKSPACE = -7
+FEM_ERR_BREAKDOWN = -8
+
+LAYOUT_BSR = 0
+LAYOUT_CSR = 1
+
+_NAMES = {FEM_ERR_INVALID: "FEM_ERR_INVALID", FEM_ERR_CUDA: "FEM_ERR_CUDA",
+          FEM_ERR_PATTERN: "FEM_ERR_PATTERN", FEM_ERR_NOT_CONVERGED: "FEM_ERR_NOT_CONVERGED",
+          FEM_ERR_MAXITER: "FEM_ERR_MAXITER", FEM_ERR_NOT_SPD: "FEM_ERR_NOT_SPD",
+          FEM_ERR_WORKSPACE: "FEM_ERR_WORKSPACE", FEM_ERR_BREAKDOWN: "FEM_ERR_BREAKDOWN"}
+
+
+class FemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class FemMesh(ctypes.Structure):
+    _fields_ = [("n_node", c_int64), ("n_elem", c_int64), ("nnzb", c_int64),
+                ("xyz", c_void_p), ("conn", c_void_p), ("indptr", c_void_p), ("indices", c_void_p),
+                ("ne_ptr", c_void_p), ("ne_list", c_void_p)]
+
+
+class FemMaterial(ctypes.Structure):
+    _fields_ = [("DE", c_double), ("EX", c_double), ("PO", c_double), ("omega", c_double * 3)]
+
+
+class FemAssemblyOut(ctypes.Structure):
+    _fields_ = [("k_layout", c_int), ("m_layout", c_int), ("K", c_void_p), ("M", c_void_p),
+                ("F", c_void_p), ("fixed", c_void_p), ("loads", c_void_p)]
+
+
+# name -> (restype, argtypes); every exported symbol of include/fem_gb300.h
+SIGNATURES = {
+    "fem_last_error": (ctypes.c_char_p, []),
+    "fem_abi_version": (c_int, []),
+    "fem_pattern_count": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p]),
+    "fem_pattern_fill": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p]),
+    "fem_incidence_build": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_assemble_workspace_bytes": (c_size_t, [c_int64]),
+    "fem_assemble": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial),
+                             ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t, c_void_p]),
+    "fem_assemble_elements": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_size_t,
+                                      c_void_p]),
+    "fem_assemble_gather": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t,
+                                    c_void_p]),
+    "fem_diag_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p]),
+    "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_stress_workspace_bytes": (c_size_t, [c_int64]),
+    "fem_stress": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
+                           c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building in-tree first if needed) and type the library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError(f"libfemgb.so not found at {_build.LIB}; run fem_taichi_gb300.build.build()")
+        L = ctypes.CDLL(_build.LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != FEM_OK:
+        msg = load().fem_last_error().decode(errors="replace")
+        raise FemError(rc, f"{what}: {msg}" if what else msg)

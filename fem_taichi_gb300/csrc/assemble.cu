@@ -1,0 +1,480 @@
+// Hex8 K / M / F assembly for sm_103a.
+//
+// Two kernels, both deterministic and free of floating-point atomics:
+//
+//  1. k_hex8_element -- 8 threads per element.  Phase A: thread g handles Gauss point g
+//     (Jacobian, adjugate, determinant, the 8 scaled gradients R_a = dN_a/dxi . adj(J),
+//     and the centrifugal load density); results are staged in shared memory.  Phase B:
+//     the 36 node pairs (a <= b) are split across the 8 threads; each accumulates the
+//     Gram matrix P_ab = sum_g R_a R_b^T / det_g and turns it into the 3x3 stiffness
+//     block  K_ab[p][q] = lam P[p][q] + mu P[q][p],  K_ab[p][p] = D0d P[p][p] + mu (tr P - P[p][p]),
+//     which equals sum_g det (B1_a^T D0 B1_b + B2_a^T D1 B2_b) of the reference
+//     (FEM_model_bsr.py:262-274, 303-347) with a different summation order.  The
+//     consistent mass M_ab = DE sum_g det_g N_a N_b (FEM_model_bsr.py:276-287) and the
+//     centrifugal load F_a (FEM_model_bsr.py:229-245, 291-300) are produced alongside.
+//     Each element writes one 3 KB record: 36 x (K 3x3 + M) and 8 x F(3).
+//
+//  2. k_gather -- one warp per block row i.  Lane l owns slot l of the row (column node
+//     indices[indptr[i] + l]).  The warp walks the incident (element, corner) list of
+//     node i in ascending element order, and each lane adds the element block whose
+//     column corner matches its column node.  The fixed order makes the sums
+//     reproducible bit for bit.  The penalty (FEM_model_bsr.py:248-259) and nodal loads
+//     (LoadF, :220-226) are applied in the same pass, and the row is written in either
+//     the BSR block order or the reference's scalar-CSR order (FEM_model_csr.py:150-173).
+#include "fem_common.cuh"
+
+namespace fem {
+namespace {
+
+constexpr int kEpc = 16;                 // elements per CTA in the element kernel
+constexpr int kElemThreads = kEpc * 8;   // 8 threads per element
+constexpr int kRec = 384;                // doubles per element record
+constexpr int kPairStride = 10;          // K (9) + M (1)
+constexpr int kFOff = 36 * kPairStride;  // 360: F block offset within a record
+constexpr int kRPad = 25;                // padded row (24 used) to spread smem banks
+
+struct ElemParams {
+    const double* xyz;
+    const int4* conn4;
+    int64_t n_elem;
+    double* rec;
+    double DE, D0d, lam, mu;
+    double w0, w1, w2;
+    DevTables tab;
+};
+
+struct ElemSmem {
+    double dnr[8][8][3];
+    double nr[8][8];
+    double x[kEpc][8][3];
+    double R[kEpc][8][kRPad];   // R_a(g)[i] at [el][g][3a+i]
+    double Rs[kEpc][8][kRPad];  // R_a(g)[i] / det_g
+    double det[kEpc][8];
+    double c[kEpc][8][3];       // DE * det_g * f(x(g))
+};
+
+// Off-diagonal pair list (a < b), 28 entries; thread t takes entries t, t+8, t+16, t+24.
+__device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
+    // q -> (a, b) for row-major enumeration of a < b
+    int aa = 0, rem = q;
+    while (rem >= 7 - aa) {
+        rem -= 7 - aa;
+        ++aa;
+    }
+    a = aa;
+    b = aa + 1 + rem;
+}
+
+__global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ElemSmem& s = *reinterpret_cast<ElemSmem*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int el = tid >> 3;
+    const int t = tid & 7;
+    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.n_elem;
+
+    for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
+    for (int k = tid; k < 64; k += kElemThreads) (&s.nr[0][0])[k] = (&p.tab.nr[0][0])[k];
+    if (valid) {
+        const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
+        const int node = __ldg(cn + t);
+        s.x[el][t][0] = __ldg(p.xyz + 3 * int64_t(node) + 0);
+        s.x[el][t][1] = __ldg(p.xyz + 3 * int64_t(node) + 1);
+        s.x[el][t][2] = __ldg(p.xyz + 3 * int64_t(node) + 2);
+    }
+    __syncthreads();
+
+    // ---- phase A: Gauss point g = t ------------------------------------------------
+    if (valid) {
+        const int g = t;
+        double J[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double acc = 0.0;
+#pragma unroll
+                for (int a = 0; a < 8; ++a) acc = fma(s.x[el][a][i], s.dnr[g][a][d], acc);
+                J[i][d] = acc;
+            }
+        double A[3][3];  // adjugate: inverse(J) = A / det
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+                A[j][i] = J[i1][j1] * J[i2][j2] - J[i2][j1] * J[i1][j2];
+            }
+        const double det = J[0][0] * A[0][0] + J[1][0] * A[0][1] + J[2][0] * A[0][2];
+        const double inv = 1.0 / det;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const double r = s.dnr[g][a][0] * A[0][i] + s.dnr[g][a][1] * A[1][i] + s.dnr[g][a][2] * A[2][i];
+                s.R[el][g][3 * a + i] = r;
+                s.Rs[el][g][3 * a + i] = r * inv;
+            }
+        s.det[el][g] = det;
+        double X[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int a = 0; a < 8; ++a) acc = fma(s.nr[g][a], s.x[el][a][i], acc);
+            X[i] = acc;
+        }
+        const double w0 = p.w0, w1 = p.w1, w2 = p.w2;
+        const double f0 = w1 * w1 * X[0] + w2 * w2 * X[0] - w0 * w1 * X[1] - w0 * w2 * X[2];
+        const double f1 = w0 * w0 * X[1] + w2 * w2 * X[1] - w1 * w2 * X[2] - w1 * w0 * X[0];
+        const double f2 = w1 * w1 * X[2] + w0 * w0 * X[2] - w2 * w0 * X[0] - w2 * w1 * X[1];
+        const double jd = p.DE * det;
+        s.c[el][g][0] = jd * f0;
+        s.c[el][g][1] = jd * f1;
+        s.c[el][g][2] = jd * f2;
+    }
+    __syncthreads();
+    if (!valid) return;
+
+    // ---- phase B: node pairs -----------------------------------------------------------
+    double* rec = p.rec + e * kRec;
+    const double lam = p.lam, mu = p.mu, D0d = p.D0d, DE = p.DE;
+    // diagonal pair (t, t): P symmetric
+    {
+        const int a = t;
+        double P00 = 0, P11 = 0, P22 = 0, P01 = 0, P02 = 0, P12 = 0, m = 0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const double r0 = s.R[el][g][3 * a], r1 = s.R[el][g][3 * a + 1], r2 = s.R[el][g][3 * a + 2];
+            const double q0 = s.Rs[el][g][3 * a], q1 = s.Rs[el][g][3 * a + 1], q2 = s.Rs[el][g][3 * a + 2];
+            P00 = fma(q0, r0, P00);
+            P11 = fma(q1, r1, P11);
+            P22 = fma(q2, r2, P22);
+            P01 = fma(q0, r1, P01);
+            P02 = fma(q0, r2, P02);
+            P12 = fma(q1, r2, P12);
+            m = fma(s.det[el][g], s.nr[g][a] * s.nr[g][a], m);
+        }
+        const double lm = lam + mu;
+        double* o = rec + pair_index(a, a) * kPairStride;
+        o[0] = D0d * P00 + mu * (P11 + P22);
+        o[4] = D0d * P11 + mu * (P00 + P22);
+        o[8] = D0d * P22 + mu * (P00 + P11);
+        o[1] = o[3] = lm * P01;
+        o[2] = o[6] = lm * P02;
+        o[5] = o[7] = lm * P12;
+        o[9] = DE * m;
+    }
+    // off-diagonal pairs
+    for (int q = t; q < 28; q += 8) {
+        int a, b;
+        offdiag_pair(q, a, b);
+        double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double m = 0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const double q0 = s.Rs[el][g][3 * a], q1 = s.Rs[el][g][3 * a + 1], q2 = s.Rs[el][g][3 * a + 2];
+            const double r0 = s.R[el][g][3 * b], r1 = s.R[el][g][3 * b + 1], r2 = s.R[el][g][3 * b + 2];
+            P[0][0] = fma(q0, r0, P[0][0]);
+            P[0][1] = fma(q0, r1, P[0][1]);
+            P[0][2] = fma(q0, r2, P[0][2]);
+            P[1][0] = fma(q1, r0, P[1][0]);
+            P[1][1] = fma(q1, r1, P[1][1]);
+            P[1][2] = fma(q1, r2, P[1][2]);
+            P[2][0] = fma(q2, r0, P[2][0]);
+            P[2][1] = fma(q2, r1, P[2][1]);
+            P[2][2] = fma(q2, r2, P[2][2]);
+            m = fma(s.det[el][g], s.nr[g][a] * s.nr[g][b], m);
+        }
+        double* o = rec + pair_index(a, b) * kPairStride;
+        o[0] = D0d * P[0][0] + mu * (P[1][1] + P[2][2]);
+        o[4] = D0d * P[1][1] + mu * (P[0][0] + P[2][2]);
+        o[8] = D0d * P[2][2] + mu * (P[0][0] + P[1][1]);
+        o[1] = lam * P[0][1] + mu * P[1][0];
+        o[2] = lam * P[0][2] + mu * P[2][0];
+        o[3] = lam * P[1][0] + mu * P[0][1];
+        o[5] = lam * P[1][2] + mu * P[2][1];
+        o[6] = lam * P[2][0] + mu * P[0][2];
+        o[7] = lam * P[2][1] + mu * P[1][2];
+        o[9] = DE * m;
+    }
+    // element load for corner t
+    {
+        double f0 = 0, f1 = 0, f2 = 0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const double n = s.nr[g][t];
+            f0 = fma(n, s.c[el][g][0], f0);
+            f1 = fma(n, s.c[el][g][1], f1);
+            f2 = fma(n, s.c[el][g][2], f2);
+        }
+        rec[kFOff + 3 * t + 0] = f0;
+        rec[kFOff + 3 * t + 1] = f1;
+        rec[kFOff + 3 * t + 2] = f2;
+    }
+}
+
+struct GatherParams {
+    int64_t n_node;
+    const int32_t* indptr;
+    const int32_t* indices;
+    const int32_t* ne_ptr;
+    const int32_t* ne_list;
+    const int4* conn4;
+    const double* rec;
+    int k_layout, m_layout;
+    double* K;
+    double* M;
+    double* F;
+    const uint8_t* fixed;
+    const double* loads;
+};
+
+__device__ __forceinline__ unsigned corner_match(int col, const int4& c0, const int4& c1) {
+    return unsigned(c0.x == col) | (unsigned(c0.y == col) << 1) | (unsigned(c0.z == col) << 2) |
+           (unsigned(c0.w == col) << 3) | (unsigned(c1.x == col) << 4) | (unsigned(c1.y == col) << 5) |
+           (unsigned(c1.z == col) << 6) | (unsigned(c1.w == col) << 7);
+}
+
+__global__ void __launch_bounds__(256) k_gather(const GatherParams p) {
+    const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= p.n_node) return;
+    const int64_t rs = p.indptr[row];
+    const int L = p.indptr[row + 1] - int(rs);
+    const int ks = p.ne_ptr[row], ke = p.ne_ptr[row + 1];
+    const unsigned fixed_bits = p.fixed ? p.fixed[row] : 0u;
+
+    for (int base = 0; base < L; base += 32) {
+        const int l = base + lane;
+        const bool active = l < L;
+        const int col = active ? __ldg(p.indices + rs + l) : -1;
+        double acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+        double accm = 0.0;
+        for (int k = ks; k < ke; ++k) {
+            const int ent = __ldg(p.ne_list + k);
+            const int64_t e = ent >> 3;
+            const int a = ent & 7;
+            const int4 c0 = __ldg(p.conn4 + 2 * e), c1 = __ldg(p.conn4 + 2 * e + 1);
+            unsigned mask = corner_match(col, c0, c1);
+            while (mask) {
+                const int b = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int lo = min(a, b), hi = max(a, b);
+                const double2* blk = reinterpret_cast<const double2*>(p.rec + e * kRec + pair_index(lo, hi) * kPairStride);
+                const double2 v0 = __ldg(blk), v1 = __ldg(blk + 1), v2 = __ldg(blk + 2), v3 = __ldg(blk + 3),
+                              v4 = __ldg(blk + 4);
+                double v[10] = {v0.x, v0.y, v1.x, v1.y, v2.x, v2.y, v3.x, v3.y, v4.x, v4.y};
+                if (a <= b) {
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) acc[k] += v[k];
+                } else {
+#pragma unroll
+                    for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+                        for (int qq = 0; qq < 3; ++qq) acc[3 * pp + qq] += v[3 * qq + pp];
+                }
+                accm += v[9];
+            }
+        }
+        if (col == int(row)) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if ((fixed_bits >> d) & 1u) acc[4 * d] = 1e20;
+        }
+        if (active) {
+            if (p.K) {
+                if (p.k_layout == FEM_LAYOUT_BSR) {
+                    double* o = p.K + 9 * (rs + l);
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) o[k] = acc[k];
+                } else {
+#pragma unroll
+                    for (int pp = 0; pp < 3; ++pp) {
+                        double* o = p.K + 9 * rs + int64_t(3 * pp) * L + 3 * l;
+                        o[0] = acc[3 * pp];
+                        o[1] = acc[3 * pp + 1];
+                        o[2] = acc[3 * pp + 2];
+                    }
+                }
+            }
+            if (p.M) {
+                if (p.m_layout == FEM_LAYOUT_BSR) {
+                    p.M[rs + l] = accm;
+                } else {
+#pragma unroll
+                    for (int pp = 0; pp < 3; ++pp) p.M[3 * rs + int64_t(pp) * L + l] = accm;
+                }
+            }
+        }
+    }
+    if (p.F && lane < 3) {
+        double f = 0.0;
+        for (int k = ks; k < ke; ++k) {
+            const int ent = __ldg(p.ne_list + k);
+            f += __ldg(p.rec + int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + lane);
+        }
+        if (p.loads) f += p.loads[3 * row + lane];
+        p.F[3 * row + lane] = f;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_csr_index(int64_t n_node, const int32_t* __restrict__ indptr,
+                                                   const int32_t* __restrict__ indices, int32_t* rowK,
+                                                   int32_t* colK, int32_t* rowM, int32_t* colM) {
+    const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n_node) return;
+    const int64_t rs = indptr[row];
+    const int L = indptr[row + 1] - int(rs);
+    if (lane < 3) {
+        // InstallIndexK / InstallIndexM: FEM_model_csr.py:167-173, 195-201
+        if (rowK) rowK[3 * row + 1 + lane] = int32_t(L * 3 * (lane + 1) + rs * 9);
+        if (rowM) rowM[3 * row + 1 + lane] = int32_t(L * (lane + 1) + rs * 3);
+        if (row == 0) {
+            if (rowK) rowK[0] = 0;
+            if (rowM) rowM[0] = 0;
+        }
+    }
+    for (int l = lane; l < L; l += 32) {
+        const int col = indices[rs + l];
+        for (int pp = 0; pp < 3; ++pp) {
+            if (colK) {
+                int32_t* o = colK + 9 * rs + int64_t(3 * pp) * L + 3 * l;
+                o[0] = 3 * col;
+                o[1] = 3 * col + 1;
+                o[2] = 3 * col + 2;
+            }
+            if (colM) colM[3 * rs + int64_t(pp) * L + l] = 3 * col + pp;
+        }
+    }
+}
+
+int check_mesh(const fem_mesh* m) {
+    FEM_REQUIRE(m != nullptr, "mesh is NULL");
+    FEM_REQUIRE(m->n_node >= 0 && m->n_elem >= 0 && m->nnzb >= 0, "negative mesh size");
+    FEM_REQUIRE(m->n_elem < (int64_t(1) << 28), "n_elem too large");
+    FEM_REQUIRE(m->n_node < (int64_t(1) << 31) - 1, "n_node too large");
+    FEM_REQUIRE(9 * m->nnzb < (int64_t(1) << 62), "nnzb too large");
+    if (m->n_elem) FEM_REQUIRE(m->xyz && m->conn && aligned16(m->conn), "xyz/conn NULL or conn not 16-byte aligned");
+    if (m->n_node) FEM_REQUIRE(m->indptr && m->ne_ptr && m->ne_list, "pattern/incidence arrays are NULL");
+    if (m->nnzb) FEM_REQUIRE(m->indices != nullptr, "indices is NULL");
+    return FEM_OK;
+}
+
+}  // namespace
+
+}  // namespace fem
+
+using namespace fem;
+
+extern "C" size_t fem_assemble_workspace_bytes(int64_t n_elem) {
+    return n_elem > 0 ? size_t(n_elem) * kRec * sizeof(double) : 0;
+}
+
+namespace {
+
+int check_assembly_inputs(const fem_mesh* mesh, const fem_material* mat, void* workspace, size_t workspace_bytes) {
+    int rc = check_mesh(mesh);
+    if (rc) return rc;
+    FEM_REQUIRE(mat != nullptr, "mat is NULL");
+    FEM_REQUIRE(mat->PO > -1.0 && mat->PO < 0.5, "Poisson ratio must lie in (-1, 0.5)");
+    if (workspace_bytes < fem_assemble_workspace_bytes(mesh->n_elem) || (mesh->n_elem && !workspace)) {
+        set_error("workspace too small: need %zu bytes", fem_assemble_workspace_bytes(mesh->n_elem));
+        return FEM_ERR_WORKSPACE;
+    }
+    FEM_REQUIRE(workspace == nullptr || aligned16(workspace), "workspace not 16-byte aligned");
+    return FEM_OK;
+}
+
+}  // namespace
+
+extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
+    if (rc) return rc;
+    if (mesh->n_elem == 0) return FEM_OK;
+    ElemParams ep;
+    ep.xyz = mesh->xyz;
+    ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+    ep.n_elem = mesh->n_elem;
+    ep.rec = static_cast<double*>(workspace);
+    const double EX = mat->EX, PO = mat->PO;
+    ep.DE = mat->DE;
+    ep.D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // FEM_model_bsr.py:435-437
+    ep.lam = EX * PO / (1 + PO) / (1 - 2 * PO);         // :439-445
+    ep.mu = EX / 2 / (1 + PO);                          // :447-449
+    ep.w0 = mat->omega[0];
+    ep.w1 = mat->omega[1];
+    ep.w2 = mat->omega[2];
+    ep.tab = make_tables();
+    const size_t smem = sizeof(ElemSmem);
+    FEM_CUDA(cudaFuncSetAttribute(k_hex8_element, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
+    k_hex8_element<<<unsigned(blocks), kElemThreads, smem, as_stream(stream)>>>(ep);
+    FEM_LAUNCH_CHECK("k_hex8_element");
+    return FEM_OK;
+}
+
+extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+    int rc = check_mesh(mesh);
+    if (rc) return rc;
+    FEM_REQUIRE(out != nullptr, "out is NULL");
+    FEM_REQUIRE(out->k_layout == FEM_LAYOUT_BSR || out->k_layout == FEM_LAYOUT_CSR, "bad k_layout");
+    FEM_REQUIRE(out->m_layout == FEM_LAYOUT_BSR || out->m_layout == FEM_LAYOUT_CSR, "bad m_layout");
+    if (workspace_bytes < fem_assemble_workspace_bytes(mesh->n_elem) || (mesh->n_elem && !workspace)) {
+        set_error("workspace too small: need %zu bytes", fem_assemble_workspace_bytes(mesh->n_elem));
+        return FEM_ERR_WORKSPACE;
+    }
+    if (mesh->n_node == 0 || (!out->K && !out->M && !out->F)) return FEM_OK;
+    GatherParams gp;
+    gp.n_node = mesh->n_node;
+    gp.indptr = mesh->indptr;
+    gp.indices = mesh->indices;
+    gp.ne_ptr = mesh->ne_ptr;
+    gp.ne_list = mesh->ne_list;
+    gp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+    gp.rec = static_cast<const double*>(workspace);
+    gp.k_layout = out->k_layout;
+    gp.m_layout = out->m_layout;
+    gp.K = out->K;
+    gp.M = out->M;
+    gp.F = out->F;
+    gp.fixed = out->fixed;
+    gp.loads = out->loads;
+    const int64_t blocks = (mesh->n_node * 32 + 255) / 256;
+    k_gather<<<unsigned(blocks), 256, 0, as_stream(stream)>>>(gp);
+    FEM_LAUNCH_CHECK("k_gather");
+    return FEM_OK;
+}
+
+extern "C" int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                            void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
+    if (rc) return rc;
+    FEM_REQUIRE(out != nullptr, "out is NULL");
+    FEM_REQUIRE(out->k_layout == FEM_LAYOUT_BSR || out->k_layout == FEM_LAYOUT_CSR, "bad k_layout");
+    FEM_REQUIRE(out->m_layout == FEM_LAYOUT_BSR || out->m_layout == FEM_LAYOUT_CSR, "bad m_layout");
+    if (mesh->n_node == 0) return FEM_OK;
+    rc = fem_assemble_elements(mesh, mat, workspace, workspace_bytes, stream);
+    if (rc) return rc;
+    return fem_assemble_gather(mesh, out, workspace, workspace_bytes, stream);
+}
+
+extern "C" int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* rowM, int32_t* colM,
+                             void* stream) {
+    FEM_REQUIRE(mesh != nullptr, "mesh is NULL");
+    FEM_REQUIRE(mesh->n_node >= 0, "negative size");
+    FEM_REQUIRE(9 * mesh->nnzb < (int64_t(1) << 31), "CSR column indices exceed int32");
+    if (mesh->n_node == 0) return FEM_OK;
+    FEM_REQUIRE(mesh->indptr && (mesh->nnzb == 0 || mesh->indices), "pattern arrays are NULL");
+    const int64_t blocks = (mesh->n_node * 32 + 255) / 256;
+    k_csr_index<<<unsigned(blocks), 256, 0, as_stream(stream)>>>(mesh->n_node, mesh->indptr, mesh->indices, rowK,
+                                                                 colK, rowM, colM);
+    FEM_LAUNCH_CHECK("k_csr_index");
+    return FEM_OK;
+}

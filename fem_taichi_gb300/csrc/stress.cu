@@ -1,0 +1,233 @@
+// Nodal stress recovery for sm_103a (POST_process.py:72-99, 172-223).
+//
+//  1. k_stress_element -- 8 threads per element.  Thread g evaluates the displacement
+//     gradient at Gauss point g as H = (sum_a u_a (x) dN_a/dxi) . adj(J) / det, and the
+//     stresses  sigma_n = D0 (H00, H11, H22),  sigma_s = mu (H01+H10, H12+H21, H02+H20)
+//     (components xy, yz, xz as UnitVectorS orders them, POST_process.py:190-209).
+//     Thread j then forms corner j's extrapolated value sum_k W[j][k] sigma(k) with the
+//     caller's 8x8 weight table (get_NdSol / shapefunc_GS, POST_process.py:172-181,
+//     212-223) and writes it to the per-element workspace.
+//  2. k_stress_node -- one thread per node: sums its incident (element, corner) values in
+//     ascending element order (no atomics), divides by the element count (get_NdAve,
+//     :183-187), then computes the principal stresses with cyclic Jacobi rotations
+//     (descending order) and the reference's "VM" formula as written (:93-94).
+#include "fem_common.cuh"
+
+namespace fem {
+namespace {
+
+constexpr int kEpc = 16;
+constexpr int kThreads = kEpc * 8;
+constexpr int kSvPad = 7;
+
+struct StressParams {
+    const double* xyz;
+    const int4* conn4;
+    const double* u;
+    int64_t n_elem;
+    double* rec;  // [n_elem][8][6]
+    double D0d, lam, mu;
+    DevTables tab;
+    double W[8][8];
+};
+
+struct StressSmem {
+    double dnr[8][8][3];
+    double W[8][8];
+    double x[kEpc][8][3];
+    double u[kEpc][8][3];
+    double sv[kEpc][8][kSvPad];
+};
+
+__global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams p) {
+    __shared__ StressSmem s;
+    const int tid = threadIdx.x;
+    const int el = tid >> 3;
+    const int t = tid & 7;
+    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.n_elem;
+    for (int k = tid; k < 8 * 8 * 3; k += kThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
+    for (int k = tid; k < 64; k += kThreads) (&s.W[0][0])[k] = (&p.W[0][0])[k];
+    if (valid) {
+        const int node = __ldg(reinterpret_cast<const int*>(p.conn4) + 8 * e + t);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s.x[el][t][i] = __ldg(p.xyz + 3 * int64_t(node) + i);
+            s.u[el][t][i] = __ldg(p.u + 3 * int64_t(node) + i);
+        }
+    }
+    __syncthreads();
+    if (valid) {
+        const int g = t;
+        double J[3][3], G[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double aj = 0.0, ag = 0.0;
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    aj = fma(s.x[el][a][i], s.dnr[g][a][d], aj);
+                    ag = fma(s.u[el][a][i], s.dnr[g][a][d], ag);
+                }
+                J[i][d] = aj;
+                G[i][d] = ag;
+            }
+        double A[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+                A[j][i] = J[i1][j1] * J[i2][j2] - J[i2][j1] * J[i1][j2];
+            }
+        const double det = J[0][0] * A[0][0] + J[1][0] * A[0][1] + J[2][0] * A[0][2];
+        const double inv = 1.0 / det;
+        double H[3][3];  // du_i/dx_k
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) H[i][k] = (G[i][0] * A[0][k] + G[i][1] * A[1][k] + G[i][2] * A[2][k]) * inv;
+        const double D0d = p.D0d, lam = p.lam, mu = p.mu;
+        s.sv[el][g][0] = D0d * H[0][0] + lam * (H[1][1] + H[2][2]);
+        s.sv[el][g][1] = D0d * H[1][1] + lam * (H[0][0] + H[2][2]);
+        s.sv[el][g][2] = D0d * H[2][2] + lam * (H[0][0] + H[1][1]);
+        s.sv[el][g][3] = mu * (H[0][1] + H[1][0]);
+        s.sv[el][g][4] = mu * (H[1][2] + H[2][1]);
+        s.sv[el][g][5] = mu * (H[0][2] + H[2][0]);
+    }
+    __syncthreads();
+    if (!valid) return;
+    const int j = t;
+    double* o = p.rec + (e * 8 + j) * 6;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc = fma(s.W[j][k], s.sv[el][k][c], acc);
+        o[c] = acc;
+    }
+}
+
+// Eigenvalues of the symmetric 3x3 [[a00,a01,a02],[a01,a11,a12],[a02,a12,a22]] by cyclic
+// Jacobi rotations (capped at 32 sweeps), returned descending.
+__device__ void sym3_eig_desc(double a00, double a11, double a22, double a01, double a12, double a02,
+                              double& p1, double& p2, double& p3) {
+    double a[3][3] = {{a00, a01, a02}, {a01, a11, a12}, {a02, a12, a22}};
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        const double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        const double dia = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+        if (off == 0.0 || off <= 1e-300 || off < 1e-17 * dia) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int pp = pq == 2 ? 1 : 0;
+            const int qq = pq == 0 ? 1 : 2;
+            const double apq = a[pp][qq];
+            if (apq == 0.0) continue;
+            const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * apq);
+            double tt;
+            if (fabs(theta) > 1e150) {
+                tt = 0.5 / theta;
+            } else {
+                tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            }
+            const double c = 1.0 / sqrt(tt * tt + 1.0), sn = tt * c;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double akp = a[k][pp], akq = a[k][qq];
+                a[k][pp] = c * akp - sn * akq;
+                a[k][qq] = sn * akp + c * akq;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double apk = a[pp][k], aqk = a[qq][k];
+                a[pp][k] = c * apk - sn * aqk;
+                a[qq][k] = sn * apk + c * aqk;
+            }
+        }
+    }
+    double e0 = a[0][0], e1 = a[1][1], e2 = a[2][2], tmp;
+    if (e0 < e1) tmp = e0, e0 = e1, e1 = tmp;
+    if (e1 < e2) tmp = e1, e1 = e2, e2 = tmp;
+    if (e0 < e1) tmp = e0, e0 = e1, e1 = tmp;
+    p1 = e0;
+    p2 = e1;
+    p3 = e2;
+}
+
+__global__ void __launch_bounds__(256) k_stress_node(int64_t n_node, const int32_t* __restrict__ ne_ptr,
+                                                     const int32_t* __restrict__ ne_list,
+                                                     const int32_t* __restrict__ co_elem,
+                                                     const double* __restrict__ rec, double* __restrict__ out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n_node) return;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const int ks = ne_ptr[i], ke = ne_ptr[i + 1];
+    for (int k = ks; k < ke; ++k) {
+        const int ent = __ldg(ne_list + k);
+        const double* r = rec + (int64_t(ent >> 3) * 8 + (ent & 7)) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v[c] += __ldg(r + c);
+    }
+    const double ce = double(co_elem[i]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = v[c] / ce;
+    double p1, p2, p3;
+    // vector order [xx, yy, zz, xy, yz, xz] (POST_process.py:79-86)
+    sym3_eig_desc(v[0], v[1], v[2], v[3], v[4], v[5], p1, p2, p3);
+    double* o = out + 10 * i;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o[c] = v[c];
+    o[6] = p1;
+    o[7] = p2;
+    o[8] = p3;
+    o[9] = sqrt((p1 - p2) * (p1 - p2) + (p2 - p3) * (p2 - p3) + (p3 - p2) * (p3 - p2));
+}
+
+}  // namespace
+}  // namespace fem
+
+using namespace fem;
+
+extern "C" size_t fem_stress_workspace_bytes(int64_t n_elem) {
+    return n_elem > 0 ? size_t(n_elem) * 48 * sizeof(double) : 0;
+}
+
+extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
+                          const double* extrap, double* out, void* workspace, size_t workspace_bytes, void* stream) {
+    FEM_REQUIRE(mesh && mat && extrap, "mesh/mat/extrap is NULL");
+    FEM_REQUIRE(mesh->n_node >= 0 && mesh->n_elem >= 0, "negative mesh size");
+    FEM_REQUIRE(mesh->n_elem < (int64_t(1) << 28), "n_elem too large");
+    FEM_REQUIRE(mat->PO > -1.0 && mat->PO < 0.5, "Poisson ratio must lie in (-1, 0.5)");
+    if (mesh->n_node == 0) return FEM_OK;
+    FEM_REQUIRE(u && co_elem && out && mesh->ne_ptr && mesh->ne_list, "u/co_elem/out/incidence is NULL");
+    if (mesh->n_elem) FEM_REQUIRE(mesh->xyz && mesh->conn && aligned16(mesh->conn), "xyz/conn NULL or misaligned");
+    if (workspace_bytes < fem_stress_workspace_bytes(mesh->n_elem) || (mesh->n_elem && !workspace)) {
+        set_error("workspace too small: need %zu bytes", fem_stress_workspace_bytes(mesh->n_elem));
+        return FEM_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    if (mesh->n_elem) {
+        StressParams sp;
+        sp.xyz = mesh->xyz;
+        sp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+        sp.u = u;
+        sp.n_elem = mesh->n_elem;
+        sp.rec = static_cast<double*>(workspace);
+        const double EX = mat->EX, PO = mat->PO;
+        sp.D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // POST_process.py:292-302
+        sp.lam = EX * PO / (1 + PO) / (1 - 2 * PO);
+        sp.mu = EX / 2 / (1 + PO);                          // :304-306
+        sp.tab = make_tables();
+        for (int j = 0; j < 8; ++j)
+            for (int k = 0; k < 8; ++k) sp.W[j][k] = extrap[8 * j + k];
+        const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
+        k_stress_element<<<unsigned(blocks), kThreads, 0, st>>>(sp);
+        FEM_LAUNCH_CHECK("k_stress_element");
+    }
+    const int64_t blocks = (mesh->n_node + 255) / 256;
+    k_stress_node<<<unsigned(blocks), 256, 0, st>>>(mesh->n_node, mesh->ne_ptr, mesh->ne_list, co_elem,
+                                                    static_cast<const double*>(workspace), out);
+    FEM_LAUNCH_CHECK("k_stress_node");
+    return FEM_OK;
+}

@@ -1,0 +1,84 @@
+"""GPU drop-in for the reference ``Post`` stress recovery (POST_process.py:14-99).
+
+``Post(name, Physics, Materials, Solutions).Get_Stress()`` returns the (N, 10) float64
+table [xx, yy, zz, xy, yz, xz, p1, p2, p3, VM] exactly as the reference lays it out
+(POST_process.py:79-95), with the reference's extrapolation convention and "VM" formula.
+
+Extrapolation table.  get_NdSol (POST_process.py:172-181) weights Gauss point k's stress
+for element corner j by shapefunc_GS(GMat[j])[k].  GMat is assigned eight corner points
+(POST_process.py:310-317) but declared with two entries (POST_process.py:145).
+``gmat_mode='written'`` (default) uses the eight assigned points; ``gmat_mode='aliased'``
+uses entry j & 1 holding the last value written to it, which is what a runtime that maps
+an out-of-range index of a 2-entry dense field onto its low bit would read.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .mesh import Physics  # noqa: F401  (type reference)
+from .model import DeviceMesh, _dptr, _stream, material
+
+GS1 = 0.57735026918962
+_GMAT_WRITTEN = np.array([[-1, -1, -1], [-1, -1, 1], [-1, 1, -1], [-1, 1, 1],
+                          [1, -1, -1], [1, -1, 1], [1, 1, -1], [1, 1, 1]], dtype=np.float64)
+
+
+def extrapolation_table(gmat_mode: str = "written") -> np.ndarray:
+    """W[j, k] = shapefunc_GS(GMat[j])[k] (POST_process.py:212-223)."""
+    if gmat_mode == "written":
+        g = _GMAT_WRITTEN
+    elif gmat_mode == "aliased":
+        g = np.array([_GMAT_WRITTEN[6 + (j & 1)] for j in range(8)])
+    else:
+        raise ValueError("gmat_mode must be 'written' or 'aliased'")
+    W = np.empty((8, 8))
+    for j in range(8):
+        a, b, c = g[j, 0] / GS1, g[j, 1] / GS1, g[j, 2] / GS1
+        W[j] = [0.125 * (1 + a) * (1 + b) * (1 - c), 0.125 * (1 - a) * (1 + b) * (1 - c),
+                0.125 * (1 - a) * (1 - b) * (1 - c), 0.125 * (1 + a) * (1 - b) * (1 - c),
+                0.125 * (1 + a) * (1 + b) * (1 + c), 0.125 * (1 - a) * (1 + b) * (1 + c),
+                0.125 * (1 - a) * (1 - b) * (1 + c), 0.125 * (1 + a) * (1 - b) * (1 + c)]
+    return W
+
+
+class Post:
+    """Drop-in for POST_process.Post (stress part)."""
+
+    def __init__(self, name, Physics, Materials, Solutions, gmat_mode="written", device="cuda", mesh=None):
+        self.name = name
+        self.DE, self.EX, self.PO = Materials['DE'], Materials['EX'], Materials['PO']
+        self.Physics = Physics
+        self.Num_Node = int(Physics.Node.shape[-1])
+        self.Num_Elem = int(Physics.Elem.shape[-1])
+        self.lib = _lib.load()
+        self.mesh = mesh if mesh is not None else DeviceMesh(Physics, device)
+        self.device = self.mesh.device
+        self.mat = material(Materials, (0.0, 0.0, 0.0))
+        self.W = np.ascontiguousarray(extrapolation_table(gmat_mode))
+        self.set_solution(Solutions)
+        self._ws = None
+
+    def set_solution(self, Solutions) -> None:
+        """Solutions: (N, 3[, 1]) host array or device tensor (POST_process.py:28: squeeze().T)."""
+        u = torch.as_tensor(Solutions).reshape(self.Num_Node, 3)
+        self.u = u.to(device=self.device, dtype=torch.float64).contiguous()
+
+    def stress_device(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        nbytes = int(self.lib.fem_stress_workspace_bytes(self.Num_Elem))
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=self.device)
+        if out is None:
+            out = torch.empty((self.Num_Node, 10), dtype=torch.float64, device=self.device)
+        W = self.W.ctypes.data_as(ctypes.c_void_p)
+        _lib.check(self.lib.fem_stress(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), _dptr(self.u),
+                                       _dptr(self.mesh.co_elem), W, _dptr(out), _dptr(self._ws), self._ws.numel(),
+                                       _stream(self.device)), "fem_stress")
+        return out
+
+    def Get_Stress(self) -> np.ndarray:
+        """POST_process.py:72-99."""
+        return self.stress_device().cpu().numpy()

@@ -1,0 +1,133 @@
+/*
+ * fem_gb300.h -- C ABI of the GB300 (sm_103a) hex8 finite-element hot path.
+ *
+ * Plain C types only: sizes are int64_t, index arrays int32_t, values double/float.
+ * Unless stated otherwise a pointer argument is a DEVICE pointer on the current CUDA
+ * device, and `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Every entry point returns an int status (FEM_OK == 0, negative on error) and never
+ * throws; fem_last_error() returns a thread-local message for the last failure.
+ * No entry point keeps global mutable state: callers own every buffer (outputs and
+ * workspaces are caller-allocated; *_workspace_bytes() tells how much to allocate).
+ *
+ * Reference interfaces replaced (tianshao1992/FEM_taichi):
+ *   fem_pattern_*          READ_physics.py:42-61       Read.pre_process (SmNode/ReNode/CoNode)
+ *   fem_incidence_build    READ_physics.py:51-60       Elem_Node incidence, CoElem
+ *   fem_assemble           FEM_model_csr.py:150-242    InstallIndexK, InstallMatrixK, InstallMatrixM,
+ *                          FEM_model_bsr.py:163-259    InstallIndexM, InstallVectorF, LoadF, ModifyK,
+ *                                                      UnitMatrixK/M, UnitVectorF, installLocalB/N
+ *   fem_csr_index          FEM_model_csr.py:163,167-173,191,195-201   RowK/ColK/RowM/ColM
+ *   fem_stress             POST_process.py:172-209,72-99  get_NdSol, get_NdAve, UnitVectorS,
+ *                                                      shapefunc_GS, Get_Stress (eigh, "VM")
+ *   fem_bsr_spmv*          SOLVE_static.py:36          KL * U (residual product)
+ *   fem_pcg_solve          SOLVE_static.py:31-33       pardisoSolver(KL, mtype=2).factor/solve
+ */
+#ifndef FEM_GB300_H
+#define FEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+#define FEM_OK 0
+#define FEM_ERR_INVALID (-1)       /* bad argument: null pointer, size, index out of range */
+#define FEM_ERR_CUDA (-2)          /* CUDA runtime error (see fem_last_error) */
+#define FEM_ERR_PATTERN (-3)       /* an element node pair is absent from the block pattern */
+#define FEM_ERR_NOT_CONVERGED (-4) /* solver stalled before reaching the tolerance */
+#define FEM_ERR_MAXITER (-5)       /* solver hit its iteration cap */
+#define FEM_ERR_NOT_SPD (-6)       /* non-positive curvature / preconditioner detected */
+#define FEM_ERR_WORKSPACE (-7)     /* workspace too small */
+#define FEM_ERR_BREAKDOWN (-8)     /* NaN/Inf encountered */
+
+#define FEM_LAYOUT_BSR 0 /* K: [nnzb][3][3] block-major;  M: [nnzb] one scalar per block      */
+#define FEM_LAYOUT_CSR 1 /* K: reference scalar CSR value order (row 3i+p: blocks m, cols q);
+                            M: reference scalar CSR with 3 entries per block, [3*nnzb]        */
+
+const char* fem_last_error(void);
+int fem_abi_version(void);
+
+/* ---- topology (HOST pointers) -------------------------------------------------- */
+/* Block-row pattern of K: row i lists, ascending, every node sharing an element with node
+ * i (itself included).  Same arrays as READ_physics.py:55-61 (SmNode = indptr,
+ * ReNode = indices).  conn: [n_elem][8] node indices in [0, n_node).
+ * fem_pattern_count fills indptr[n_node+1] and *nnzb; fem_pattern_fill fills indices. */
+int fem_pattern_count(int64_t n_node, int64_t n_elem, const int32_t* conn, int32_t* indptr,
+                      int64_t* nnzb);
+int fem_pattern_fill(int64_t n_node, int64_t n_elem, const int32_t* conn, const int32_t* indptr,
+                     int32_t* indices);
+/* Node -> element incidence: for node i, ne_list[ne_ptr[i] .. ne_ptr[i+1]) holds e*8+a for
+ * every (element e, local corner a) with conn[e][a] == i, ascending in (e, a).
+ * co_elem[i] = number of distinct elements touching node i (READ_physics.py:60). */
+int fem_incidence_build(int64_t n_node, int64_t n_elem, const int32_t* conn, int32_t* ne_ptr,
+                        int32_t* ne_list, int32_t* co_elem);
+
+/* ---- device mesh descriptor ---------------------------------------------------- */
+typedef struct fem_mesh {
+    int64_t n_node, n_elem, nnzb;
+    const double* xyz;      /* [n_node][3] */
+    const int32_t* conn;    /* [n_elem][8], 16-byte aligned */
+    const int32_t* indptr;  /* [n_node+1] */
+    const int32_t* indices; /* [nnzb] */
+    const int32_t* ne_ptr;  /* [n_node+1] */
+    const int32_t* ne_list; /* [8*n_elem] */
+} fem_mesh;
+
+typedef struct fem_material {
+    double DE, EX, PO;  /* density, Young's modulus, Poisson ratio (FEM_model_bsr.py:10) */
+    double omega[3];    /* global angular velocity about an axis through the origin      */
+} fem_material;
+
+typedef struct fem_assembly_out {
+    int k_layout;          /* FEM_LAYOUT_BSR or FEM_LAYOUT_CSR                            */
+    int m_layout;          /* FEM_LAYOUT_BSR or FEM_LAYOUT_CSR                            */
+    double* K;             /* 9*nnzb values, or NULL to skip K                           */
+    double* M;             /* nnzb (BSR) or 3*nnzb (CSR) values, or NULL to skip M        */
+    double* F;             /* [n_node][3], or NULL to skip F                             */
+    const uint8_t* fixed;  /* [n_node] bit p => DOF p of the node is penalised (K diagonal
+                              entry set to 1e20, FEM_model_bsr.py:248-259), or NULL       */
+    const double* loads;   /* [n_node][3] nodal loads added to F after the element terms
+                              (LoadF, FEM_model_bsr.py:220-226), or NULL                   */
+} fem_assembly_out;
+
+/* Assemble K, M and F for one mesh: element integrals (2x2x2 Gauss, FP64) into a
+ * per-element workspace, then a deterministic, atomic-free gather where one warp owns
+ * one block row and sums its incident elements in ascending element order. */
+size_t fem_assemble_workspace_bytes(int64_t n_elem);
+int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                 void* workspace, size_t workspace_bytes, void* stream);
+/* The two phases of fem_assemble, callable separately (same workspace): element records
+ * (UnitMatrixK/M + UnitVectorF, FEM_model_bsr.py:262-300), then the gather into K/M/F
+ * (InstallMatrixK/M, InstallVectorF scatter, LoadF, ModifyK; FEM_model_csr.py:150-242). */
+int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, void* workspace,
+                          size_t workspace_bytes, void* stream);
+int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* Reference CSR index arrays (depend on the pattern only): rowK [3N+1], colK [9 nnzb],
+ * rowM [3N+1], colM [3 nnzb]; any may be NULL. */
+int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* rowM,
+                  int32_t* colM, void* stream);
+
+/* ---- stress recovery ------------------------------------------------------------- */
+/* u: [n_node][3] displacement; co_elem: [n_node]; extrap: HOST [8][8] weights W[j][k]
+ * (node j <- Gauss point k; POST_process.py:176-181); out: [n_node][10] =
+ * [xx,yy,zz,xy,yz,xz, p1>=p2>=p3, "VM" as written at POST_process.py:93-94]. */
+size_t fem_stress_workspace_bytes(int64_t n_elem);
+int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
+               const int32_t* co_elem, const double* extrap, double* out, void* workspace,
+               size_t workspace_bytes, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------------ */
+/* Measured FP64 FMA throughput of this device (TFLOP/s, 2 flops per FMA), from a kernel of
+ * independent fma chains timed with CUDA events on `stream`.  No reference counterpart: it
+ * supplies the FP64 roofline denominator for the FP64-bound element kernels. */
+int fem_diag_fp64_tflops(double* tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEM_GB300_H */

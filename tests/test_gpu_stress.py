@@ -1,0 +1,60 @@
+"""GPU parity of nodal stress recovery against the oracle.
+
+Tolerance: stresses, principal stresses and "VM" within 1e-10 relative -- per node, the
+largest deviation over the 10 columns is at most 1e-10 x the largest |value| of that node.
+"""
+import numpy as np
+import pytest
+
+import fem_taichi_gb300 as F
+from oracle import c_oracle as C
+from oracle import fem_oracle as O
+from tests.fixtures import STEEL, mesh2_physics
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+def assert_stress_close(S, So, rel=REL):
+    assert S.shape == So.shape
+    sc = np.abs(So).max(axis=1, keepdims=True)
+    dev = np.abs(S - So)
+    assert np.all(dev <= rel * sc), f"max rel dev {np.max(dev / np.maximum(sc, 1e-300))}"
+
+
+@pytest.mark.parametrize("mode", ["written", "aliased"])
+@pytest.mark.parametrize("name", ["mesh2", "c1", "twisted"])
+def test_stress_matches_oracle(name, mode):
+    P = {"mesh2": mesh2_physics, "c1": lambda: F.config_mesh("c1"),
+         "twisted": lambda: F.hex_block(6, 5, 3, jitter=0.12, twist_deg=40, seed=4)}[name]()
+    rng = np.random.default_rng(17)
+    u = rng.uniform(-1e-3, 1e-3, size=(P.Num_Node, 3, 1))
+    S = F.Post(name, P, STEEL, u, gmat_mode=mode).Get_Stress()
+    assert_stress_close(S, O.oracle_stress(P, STEEL, u, gmat_mode=mode))
+
+
+def test_constant_stress_field_is_reproduced_exactly():
+    P = F.hex_block(5, 4, 3, jitter=0.15, seed=1)
+    Gd = np.array([[1e-3, 2e-4, -3e-4], [5e-4, -1e-3, 1e-4], [2e-4, 3e-4, 4e-4]])
+    u = P.xyz @ Gd.T
+    S = F.Post("p", P, STEEL, u).Get_Stress()
+    assert np.allclose(S, S[:1], rtol=1e-10, atol=1e-8)
+
+
+def test_isolated_node_gives_nan_like_reference():
+    """A node with no element divides 0 by CoElem = 0 (POST_process.py:186)."""
+    xyz = np.vstack([F.hex_block(1, 1, 1).xyz, [[5.0, 5.0, 5.0]]])
+    elem = F.hex_block(1, 1, 1).Elem
+    P = F.Physics(np.arange(1, 10), xyz, elem, [], [])
+    S = F.Post("i", P, STEEL, np.zeros((9, 3))).Get_Stress()
+    assert np.all(np.isnan(S[8, :6])) and np.all(np.isfinite(S[:8]))
+
+
+def test_full_size_c2_stress_against_c_oracle():
+    P = F.config_mesh("c2")
+    rng = np.random.default_rng(2)
+    u = rng.uniform(-1e-3, 1e-3, size=(P.Num_Node, 3))
+    S = F.Post("c2", P, STEEL, u).Get_Stress()
+    Sc = C.stress(P.xyz, P.conn, P.CoElem, STEEL, u, O.extrapolation_table("written"), nthreads=0)
+    assert_stress_close(S, Sc)

@@ -1,0 +1,78 @@
+"""Native pattern / incidence (host code of libfemgb.so) against the reference's scipy
+SpGEMM construction (READ_physics.py:42-61): bit-exact, including edge cases."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import fem_taichi_gb300 as F
+from fem_taichi_gb300 import _lib
+from fem_taichi_gb300.mesh import build_incidence, build_pattern
+from oracle import fem_oracle as O
+from tests.fixtures import mesh2_physics
+
+
+def _check(P):
+    T = O.pre_process(P.Node, P.Elem)
+    assert np.array_equal(T["SmNode"], P.SmNode)
+    assert np.array_equal(T["ReNode"], P.ReNode)
+    assert np.array_equal(T["CoNode"], P.CoNode)
+    assert np.array_equal(T["CoElem"], P.CoElem)
+    assert np.array_equal(T["Nind"], P.Nind)
+
+
+def test_mesh2_pattern():
+    _check(mesh2_physics())
+
+
+@pytest.mark.parametrize("cfg", ["c1"])
+def test_config_pattern(cfg):
+    _check(F.config_mesh(cfg))
+
+
+def test_twisted_and_random_order():
+    P = F.hex_block(7, 3, 2, jitter=0.05, twist_deg=30, seed=2)
+    _check(P)
+    # shuffled element order and non-contiguous node ids
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(P.Num_Elem)
+    ids = P.Node[0].astype(np.int64) * 3 + 7
+    elem = (ids[P.conn[perm]] - 1).T
+    Q = F.Physics(ids, P.xyz, elem, [], [])
+    _check(Q)
+
+
+def test_isolated_nodes_and_degenerate_element():
+    xyz = np.random.default_rng(0).random((13, 3))
+    elem = np.array([[0, 1, 2, 3, 4, 5, 6, 7], [4, 5, 6, 7, 8, 9, 10, 10]]).T   # node 10 repeated
+    Q = F.Physics(np.arange(1, 14), xyz, elem, [], [])                           # nodes 11, 12 isolated
+    _check(Q)
+    assert Q.CoNode[11] == 0 and Q.CoElem[12] == 0
+    ne_ptr, ne_list, co = build_incidence(Q.conn, Q.Num_Node)
+    assert ne_ptr[11] - ne_ptr[10] == 2 and co[10] == 1          # two corners, one element
+
+
+def test_incidence_order():
+    P = F.hex_block(4, 3, 2, seed=1)
+    ptr, lst, co = build_incidence(P.conn, P.Num_Node)
+    for i in range(P.Num_Node):
+        ent = lst[ptr[i]:ptr[i + 1]]
+        assert np.all(np.diff(ent) > 0)
+        assert np.all(P.conn[ent >> 3, ent & 7] == i)
+    assert ptr[-1] == 8 * P.Num_Elem
+
+
+def test_empty_mesh():
+    ip, ind = build_pattern(np.zeros((0, 8), np.int32), 3)
+    assert np.array_equal(ip, [0, 0, 0, 0]) and ind.size == 0
+
+
+def test_out_of_range_connectivity_is_rejected():
+    conn = np.zeros((1, 8), np.int32)
+    conn[0, 3] = 9
+    with pytest.raises(_lib.FemError) as ei:
+        build_pattern(conn, 4)
+    assert ei.value.code == _lib.FEM_ERR_INVALID
+    conn[0, 3] = -1
+    with pytest.raises(_lib.FemError):
+        build_incidence(conn, 4)
