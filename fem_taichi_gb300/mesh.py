@@ -189,6 +189,8 @@ CONFIGS = {
                load_face="zmax", load=(0, 0, -1)),
     # 200x200x24, jitter +-0.1 h, z = 0 fixed
     "c2": dict(nx=200, ny=200, nz=24, size=(200.0, 200.0, 24.0), jitter=0.1, seed=2, fix="zmin"),
+    # profiling-size member of the c2 family (100x100x24, 240,000 elements)
+    "c2s": dict(nx=100, ny=100, nz=24, size=(100.0, 100.0, 24.0), jitter=0.1, seed=2, fix="zmin"),
     # 100x100x20 stretched 4:1 in z, jitter +-0.1 h, bottom fixed, top traction (host loads)
     "c3": dict(nx=100, ny=100, nz=20, size=(100.0, 100.0, 80.0), jitter=0.1, seed=3, fix="zmin"),
     # evaluation block of the learned-preconditioner study
