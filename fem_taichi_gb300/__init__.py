@@ -8,6 +8,7 @@ all arithmetic runs in hand-written CUDA kernels behind the C ABI of ``libfemgb.
 from .mesh import CONFIGS, STEEL, Physics, Read, config_mesh, face_traction_loads, hex_block  # noqa: F401
 from .model import Model  # noqa: F401
 from .post import Post, extrapolation_table  # noqa: F401
+from .solve import DeviceSystem, Static_solver  # noqa: F401
 
 __all__ = ["Read", "Physics", "Model", "Post", "hex_block", "config_mesh", "CONFIGS", "STEEL",
-           "face_traction_loads", "extrapolation_table"]
+           "face_traction_loads", "extrapolation_table", "Static_solver", "DeviceSystem"]

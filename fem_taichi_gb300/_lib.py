@@ -29,6 +29,8 @@ FEM_ERR_BREAKDOWN = -8
 
 LAYOUT_BSR = 0
 LAYOUT_CSR = 1
+FEM_F64 = 0
+FEM_F32 = 1
 
 _NAMES = {FEM_ERR_INVALID: "FEM_ERR_INVALID", FEM_ERR_CUDA: "FEM_ERR_CUDA",
           FEM_ERR_PATTERN: "FEM_ERR_PATTERN", FEM_ERR_NOT_CONVERGED: "FEM_ERR_NOT_CONVERGED",
@@ -57,6 +59,22 @@ class FemAssemblyOut(ctypes.Structure):
                 ("F", c_void_p), ("fixed", c_void_p), ("loads", c_void_p)]
 
 
+class FemBsr(ctypes.Structure):
+    _fields_ = [("n_brow", c_int64), ("nnzb", c_int64), ("indptr", c_void_p), ("indices", c_void_p),
+                ("vals", c_void_p), ("dtype", c_int)]
+
+
+class FemPcgOpts(ctypes.Structure):
+    _fields_ = [("nrhs", c_int), ("mixed", c_int), ("rtol", c_double), ("maxit", c_int), ("inner_rtol", c_double),
+                ("inner_maxit", c_int), ("max_outer", c_int), ("use_graph", c_int), ("unroll", c_int),
+                ("spmv_variant", c_int), ("spmv_variant32", c_int)]
+
+
+class FemPcgStats(ctypes.Structure):
+    _fields_ = [("status", c_int), ("iterations", c_int), ("outer", c_int), ("relres", c_double),
+                ("time_ms", c_double)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/fem_gb300.h
 SIGNATURES = {
     "fem_last_error": (ctypes.c_char_p, []),
@@ -73,6 +91,14 @@ SIGNATURES = {
                                     c_void_p]),
     "fem_diag_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p]),
     "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_bsr_spmv": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, c_void_p]),
+    "fem_spmv_autotune": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, ctypes.POINTER(c_int),
+                                  ctypes.POINTER(ctypes.c_float), c_void_p]),
+    "fem_convert_f64_to_f32": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
+    "fem_block_jacobi": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_pcg_workspace_bytes": (c_size_t, [c_int64, c_int, c_int]),
+    "fem_pcg_solve": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,
+                              ctypes.POINTER(FemPcgOpts), ctypes.POINTER(FemPcgStats), c_void_p, c_size_t, c_void_p]),
     "fem_stress_workspace_bytes": (c_size_t, [c_int64]),
     "fem_stress": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -1,0 +1,614 @@
+// Device-resident block-preconditioned conjugate gradients on the 3x3-block BSR matrix.
+// Replaces pardisoSolver(KL, mtype=2).factor()/solve(F) of SOLVE_static.py:31-33.
+//
+// One PCG iteration is three kernels (p = z + beta p;  q = A p with p.q;  x += alpha p,
+// r -= alpha q, z = M r with r.z and r.r).  All scalars live in a device state block:
+// every reduction writes per-CTA partials and the last CTA to finish (atomic ticket) sums
+// them in CTA order, so results are bitwise reproducible, and computes alpha / beta /
+// convergence on the device.  Each kernel returns immediately once the state says the
+// solve is done, so a CUDA graph holding `unroll` iterations can be replayed without a
+// host round trip per iteration; the host reads the state once per replay and stops at
+// convergence or at the iteration cap.  Up to 32 right-hand sides run in lockstep with
+// per-RHS alpha / beta and a per-RHS convergence mask (converged systems freeze).
+//
+// Mixed precision: the inner PCG runs with an FP32 matrix, FP32 vectors and FP32
+// preconditioner blocks (dot products accumulated in FP64); an FP64 iterative-refinement
+// loop forms the true residual r = F - K u with the FP64 matrix, scales it to unit norm,
+// solves K d = r approximately in FP32, and updates u += |r| d in FP64.
+#include <algorithm>
+#include <vector>
+
+#include "spmv.cuh"
+
+namespace fem {
+
+int bsr_spmv_any(const fem_bsr* A, int nrhs, const void* x, void* y, int variant, cudaStream_t st);
+
+namespace {
+
+constexpr int kMaxR = 32;
+constexpr int kThreads = 256;
+constexpr int kMaxCtas = 4096;
+constexpr int kSlots = 3;
+
+struct PcgState {
+    double rz[kMaxR], pq[kMaxR], alpha[kMaxR], beta[kMaxR], bb[kMaxR], rr[kMaxR], tol2[kMaxR];
+    double norm2[kMaxR];
+    int active[kMaxR];
+    int iters[kMaxR];
+    int it, done, status, maxit;
+    unsigned ticket;
+};
+
+// Sum of v over the lanes of this warp that hold the same right-hand side (lane % R).
+template <int R>
+__device__ __forceinline__ double warp_rhs_sum(double v) {
+#pragma unroll
+    for (int off = 16; off >= R; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Block-level reduction of up to kSlots values per RHS into part[blockIdx.x]; returns true
+// in every thread of the CTA that finished last (after which part[] is complete).
+template <int R, int NS>
+__device__ bool block_partials(const double (&v)[NS], double* part, unsigned* ticket) {
+    __shared__ double sm[kThreads / 32][NS][kMaxR];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const double w = warp_rhs_sum<R>(v[s]);
+        if (lane < R) sm[warp][s][lane] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < R) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            double acc = 0.0;
+            for (int w = 0; w < int(blockDim.x / 32); ++w) acc += sm[w][s][threadIdx.x];
+            part[(int64_t(blockIdx.x) * kSlots + s) * kMaxR + threadIdx.x] = acc;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// In the last CTA: total over CTAs (in CTA order) of slot s for RHS k.
+__device__ __forceinline__ double total(const double* part, int nblocks, int s, int k) {
+    double acc = 0.0;
+    for (int b = 0; b < nblocks; ++b) acc += __ldcg(part + (int64_t(b) * kSlots + s) * kMaxR + k);
+    return acc;
+}
+
+// z = M r for one node / RHS, M the node's 3x3 preconditioner block.
+template <typename T>
+__device__ __forceinline__ void apply_block(const T* __restrict__ Mi, T r0, T r1, T r2, T& z0, T& z1, T& z2) {
+    z0 = Mi[0] * r0 + Mi[1] * r1 + Mi[2] * r2;
+    z1 = Mi[3] * r0 + Mi[4] * r1 + Mi[5] * r2;
+    z2 = Mi[6] * r0 + Mi[7] * r1 + Mi[8] * r2;
+}
+
+// x = 0, r = b, z = M r; rz, rr -> state (bb = rr, tol2 = rtol^2 bb).
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_init(int64_t n, const T* __restrict__ M, const T* __restrict__ b,
+                                                    T* x, T* r, T* z, double* part, PcgState* st, double rtol,
+                                                    int maxit) {
+    double v[2] = {0.0, 0.0};
+    const int64_t total_t = n * R;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < ((total_t + 31) / 32) * 32;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        if (t < total_t) {
+            const int64_t node = t / R;
+            const int k = int(t % R);
+            const int64_t o = 3 * node * R + k;
+            const T r0 = b[o], r1 = b[o + R], r2 = b[o + 2 * R];
+            T z0, z1, z2;
+            apply_block(M + 9 * node, r0, r1, r2, z0, z1, z2);
+            x[o] = 0;
+            x[o + R] = 0;
+            x[o + 2 * R] = 0;
+            r[o] = r0;
+            r[o + R] = r1;
+            r[o + 2 * R] = r2;
+            z[o] = z0;
+            z[o + R] = z1;
+            z[o + 2 * R] = z2;
+            v[0] += double(r0) * double(z0) + double(r1) * double(z1) + double(r2) * double(z2);
+            v[1] += double(r0) * double(r0) + double(r1) * double(r1) + double(r2) * double(r2);
+        }
+    }
+    if (block_partials<R, 2>(v, part, &st->ticket) && threadIdx.x == 0) {
+        int any = 0, status = FEM_OK;
+        for (int k = 0; k < kMaxR; ++k) {
+            double rz = 0.0, rr = 0.0;
+            if (k < R) {
+                rz = total(part, gridDim.x, 0, k);
+                rr = total(part, gridDim.x, 1, k);
+            }
+            const bool finite = isfinite(rz) && isfinite(rr);
+            if (!finite) status = FEM_ERR_BREAKDOWN;
+            st->rz[k] = rz;
+            st->bb[k] = rr;
+            st->rr[k] = rr;
+            st->tol2[k] = rtol * rtol * rr;
+            st->active[k] = (k < R && finite && rr > 0.0) ? 1 : 0;
+            st->beta[k] = 0.0;
+            st->alpha[k] = 0.0;
+            st->iters[k] = 0;
+            any |= st->active[k];
+        }
+        st->it = 0;
+        st->done = !any;
+        st->status = status;
+        st->maxit = maxit;
+        st->ticket = 0;
+    }
+}
+
+// p = z + beta p  (p = z on the first iteration)
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_p_update(int64_t nv, const T* __restrict__ z, T* p,
+                                                        const PcgState* __restrict__ st) {
+    if (st->done) return;
+    const bool first = st->it == 0;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nv; e += int64_t(gridDim.x) * blockDim.x) {
+        const int k = int(e % R);
+        p[e] = first ? z[e] : T(z[e] + T(st->beta[k]) * p[e]);
+    }
+}
+
+// q = A p and p.q -> alpha = rz / pq on the device.
+template <typename T, int LPR_OR_R>
+__global__ void __launch_bounds__(kThreads) k_spmv_pq(const BsrView<T> A, const T* __restrict__ p, T* __restrict__ q,
+                                                       double* part, PcgState* st, int R) {
+    if (st->done) return;
+    double v[1];
+    if (R == 1)
+        v[0] = spmv1_rows<T, LPR_OR_R>(A, p, q, true);
+    else
+        v[0] = spmm_rows<T, LPR_OR_R>(A, p, q, true);
+    bool last;
+    if (R == 1)
+        last = block_partials<1, 1>(v, part, &st->ticket);
+    else
+        last = block_partials<LPR_OR_R, 1>(v, part, &st->ticket);
+    if (last) {
+        const int k = threadIdx.x;
+        if (k < R) {
+            if (st->active[k]) {
+                const double pq = total(part, gridDim.x, 0, k);
+                st->pq[k] = pq;
+                if (pq > 0.0 && isfinite(pq)) {
+                    st->alpha[k] = st->rz[k] / pq;
+                } else {
+                    st->alpha[k] = 0.0;
+                    st->active[k] = 0;
+                    st->status = isfinite(pq) ? FEM_ERR_NOT_SPD : FEM_ERR_BREAKDOWN;
+                }
+            } else {
+                st->alpha[k] = 0.0;  // converged systems stay frozen
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) st->ticket = 0;
+    }
+}
+
+// x += alpha p; r -= alpha q; z = M r; rz, rr -> beta, convergence, iteration count.
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_update(int64_t n, const T* __restrict__ M, const T* __restrict__ p,
+                                                      const T* __restrict__ q, T* x, T* r, T* z, double* part,
+                                                      PcgState* st) {
+    if (st->done) return;
+    double v[2] = {0.0, 0.0};
+    const int64_t total_t = n * R;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < ((total_t + 31) / 32) * 32;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        if (t < total_t) {
+            const int64_t node = t / R;
+            const int k = int(t % R);
+            const int64_t o = 3 * node * R + k;
+            const T a = T(st->alpha[k]);
+            x[o] += a * p[o];
+            x[o + R] += a * p[o + R];
+            x[o + 2 * R] += a * p[o + 2 * R];
+            const T r0 = r[o] - a * q[o], r1 = r[o + R] - a * q[o + R], r2 = r[o + 2 * R] - a * q[o + 2 * R];
+            r[o] = r0;
+            r[o + R] = r1;
+            r[o + 2 * R] = r2;
+            T z0, z1, z2;
+            apply_block(M + 9 * node, r0, r1, r2, z0, z1, z2);
+            z[o] = z0;
+            z[o + R] = z1;
+            z[o + 2 * R] = z2;
+            v[0] += double(r0) * double(z0) + double(r1) * double(z1) + double(r2) * double(z2);
+            v[1] += double(r0) * double(r0) + double(r1) * double(r1) + double(r2) * double(r2);
+        }
+    }
+    if (block_partials<R, 2>(v, part, &st->ticket)) {
+        const int k = threadIdx.x;
+        if (k < R && st->active[k]) {
+            const double rz = total(part, gridDim.x, 0, k), rr = total(part, gridDim.x, 1, k);
+            st->beta[k] = rz / st->rz[k];
+            st->rz[k] = rz;
+            st->rr[k] = rr;
+            st->iters[k] += 1;
+            if (!(rr > st->tol2[k])) st->active[k] = 0;
+            if (!isfinite(rr)) {
+                st->active[k] = 0;
+                st->status = FEM_ERR_BREAKDOWN;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int kk = 0; kk < R; ++kk) any |= st->active[kk];
+            st->it += 1;
+            if (any && st->it >= st->maxit) {
+                st->status = st->status ? st->status : FEM_ERR_MAXITER;
+                any = 0;
+            }
+            st->done = !any;
+            st->ticket = 0;
+        }
+    }
+}
+
+// ---- FP64 refinement helpers --------------------------------------------------------------
+// r = b - y (y = A u computed by the SpMV), norms of r per RHS -> st->norm2.
+template <int R>
+__global__ void __launch_bounds__(kThreads) k_residual(int64_t nv, const double* __restrict__ b,
+                                                        const double* __restrict__ y, double* r, double* part,
+                                                        PcgState* st) {
+    double v[1] = {0.0};
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ((nv + 31) / 32) * 32;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        if (e < nv) {
+            const double d = b[e] - y[e];
+            r[e] = d;
+            v[0] += d * d;
+        }
+    }
+    if (block_partials<R, 1>(v, part, &st->ticket)) {
+        if (threadIdx.x < R) st->norm2[threadIdx.x] = total(part, gridDim.x, 0, threadIdx.x);
+        __syncthreads();
+        if (threadIdx.x == 0) st->ticket = 0;
+    }
+}
+
+// b32 = r / s_k (s_k = 0 -> zero right-hand side)
+template <int R>
+__global__ void k_scale_cast(int64_t nv, const double* __restrict__ r, const double* __restrict__ s, float* b32) {
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nv; e += int64_t(gridDim.x) * blockDim.x) {
+        const double sk = s[e % R];
+        b32[e] = sk > 0.0 ? float(r[e] / sk) : 0.0f;
+    }
+}
+
+// u += s_k d
+template <int R>
+__global__ void k_axpy_cast(int64_t nv, const double* __restrict__ s, const float* __restrict__ d, double* u) {
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nv; e += int64_t(gridDim.x) * blockDim.x)
+        u[e] += s[e % R] * double(d[e]);
+}
+
+__global__ void k_zero(int64_t n, double* u) {
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += int64_t(gridDim.x) * blockDim.x)
+        u[e] = 0.0;
+}
+
+// ---- host side ------------------------------------------------------------------------------
+struct Layout {
+    size_t state, part, v64[5], v32[6], m32, scale, total;
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+Layout layout(int64_t n, int R, int mixed) {
+    Layout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += align_up(bytes);
+        return o;
+    };
+    const size_t nv = size_t(3) * n * R;
+    L.state = take(sizeof(PcgState));
+    L.part = take(sizeof(double) * kMaxCtas * kSlots * kMaxR);
+    for (int i = 0; i < 5; ++i) L.v64[i] = take(mixed ? (i < 2 ? sizeof(double) * nv : 0) : sizeof(double) * nv);
+    for (int i = 0; i < 6; ++i) L.v32[i] = take(mixed ? sizeof(float) * nv : 0);
+    L.m32 = take(mixed ? sizeof(float) * 9 * n : 0);
+    L.scale = take(sizeof(double) * kMaxR);
+    L.total = off;
+    return L;
+}
+
+unsigned vec_grid(int64_t work) {
+    const int64_t need = (work + kThreads - 1) / kThreads;
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>(need, std::min<int64_t>(kMaxCtas, int64_t(sm_count()) * 8))));
+}
+
+template <typename T>
+unsigned spmv_grid(int64_t n, int R, int variant) {
+    int64_t rows_per_cta, cap;
+    if (R == 1) {
+        const SpmvVariant v = spmv_variant(variant);
+        rows_per_cta = int64_t(kThreads / 32) * (32 / v.lpr);
+        cap = int64_t(sm_count()) * (v.ctas_per_sm * v.threads / kThreads);
+    } else {
+        rows_per_cta = int64_t(kThreads / 32) * (32 / R);
+        cap = int64_t(sm_count()) * 8;
+    }
+    const int64_t need = (n + rows_per_cta - 1) / rows_per_cta;
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>({need, cap, int64_t(kMaxCtas)})));
+}
+
+template <typename T, int R>
+void launch_spmv_pq(const BsrView<T>& A, const T* p, T* q, double* part, PcgState* st, int variant, cudaStream_t s) {
+    const unsigned g = spmv_grid<T>(A.n, R, variant);
+    if (R > 1) {
+        k_spmv_pq<T, R><<<g, kThreads, 0, s>>>(A, p, q, part, st, R);
+        return;
+    }
+    switch (spmv_variant(variant).lpr) {
+        case 32: k_spmv_pq<T, 32><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+        case 16: k_spmv_pq<T, 16><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+        default: k_spmv_pq<T, 8><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+    }
+}
+
+template <typename T, int R>
+int launch_iterations(const BsrView<T>& A, const T* M, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
+                      int variant, int count, cudaStream_t s) {
+    const int64_t nv = 3 * A.n * R;
+    const unsigned gv = vec_grid(nv), gn = vec_grid(A.n * R);
+    for (int i = 0; i < count; ++i) {
+        k_p_update<T, R><<<gv, kThreads, 0, s>>>(nv, z, p, st);
+        launch_spmv_pq<T, R>(A, p, q, part, st, variant, s);
+        k_update<T, R><<<gn, kThreads, 0, s>>>(A.n, M, p, q, x, r, z, part, st);
+    }
+    FEM_LAUNCH_CHECK("pcg iteration");
+    return FEM_OK;
+}
+
+struct InnerResult {
+    int iters, status;
+};
+
+// Runs PCG on (A, M) with right-hand side b into x; vectors r z p q are workspace.
+template <typename T, int R>
+int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
+             double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res) {
+    k_init<T, R><<<vec_grid(A.n * R), kThreads, 0, s>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
+    FEM_LAUNCH_CHECK("k_init");
+    unroll = std::max(1, std::min(unroll, 256));
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        cudaGraph_t g = nullptr;
+        FEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, unroll, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (rc) return rc;
+        FEM_CUDA(ce);
+        ce = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        FEM_CUDA(ce);
+    }
+    PcgState h;
+    int launched = 0, rc = FEM_OK;
+    // the device caps iterations at maxit; the host loop is bounded by the same count
+    while (launched < maxit + unroll) {
+        if (exec) {
+            rc = cuda_status(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+        } else {
+            rc = launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, unroll, s);
+        }
+        if (rc) break;
+        launched += unroll;
+        rc = cuda_status(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s), "state copy");
+        if (rc) break;
+        rc = cuda_status(cudaStreamSynchronize(s), "state sync");
+        if (rc || h.done) break;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    res->iters = h.it;
+    res->status = h.done ? h.status : FEM_ERR_MAXITER;
+    return FEM_OK;
+}
+
+template <int R>
+int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const double* F, double* U,
+            const fem_pcg_opts* o, fem_pcg_stats* out, unsigned char* ws, cudaStream_t s) {
+    const int64_t n = A64->n_brow;
+    const int64_t nv = 3 * n * R;
+    const Layout L = layout(n, R, o->mixed);
+    PcgState* st = reinterpret_cast<PcgState*>(ws + L.state);
+    double* part = reinterpret_cast<double*>(ws + L.part);
+    BsrView<double> K64{n, A64->indptr, A64->indices, static_cast<const double*>(A64->vals)};
+    const int maxit = std::max(1, o->maxit);
+    InnerResult ir{0, FEM_OK};
+    PcgState h;
+    auto true_residual = [&](const double* u, double* y, double* r) -> int {
+        int rc = bsr_spmv_any(A64, R, u, y, o->spmv_variant, s);
+        if (rc) return rc;
+        k_residual<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, F, y, r, part, st);
+        FEM_LAUNCH_CHECK("k_residual");
+        FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+        FEM_CUDA(cudaStreamSynchronize(s));
+        return FEM_OK;
+    };
+    double bnorm[kMaxR];
+    {
+        // ||F_k||: residual of u = 0
+        double* y = reinterpret_cast<double*>(ws + L.v64[0]);
+        double* r = reinterpret_cast<double*>(ws + L.v64[1]);
+        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, y);
+        k_residual<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, F, y, r, part, st);
+        FEM_LAUNCH_CHECK("k_residual");
+        FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+        FEM_CUDA(cudaStreamSynchronize(s));
+        for (int k = 0; k < R; ++k) bnorm[k] = sqrt(h.norm2[k]);
+    }
+    int total_iters = 0, outer = 0, status = FEM_OK;
+    if (!o->mixed) {
+        double* r = reinterpret_cast<double*>(ws + L.v64[0]);
+        double* z = reinterpret_cast<double*>(ws + L.v64[1]);
+        double* p = reinterpret_cast<double*>(ws + L.v64[2]);
+        double* q = reinterpret_cast<double*>(ws + L.v64[3]);
+        int rc = pcg_core<double, R>(K64, M64, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
+                                     o->use_graph, o->unroll, s, &ir);
+        if (rc) return rc;
+        total_iters = ir.iters;
+        outer = 1;
+        status = ir.status;
+        rc = true_residual(U, q, r);
+        if (rc) return rc;
+    } else {
+        BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals)};
+        double* y = reinterpret_cast<double*>(ws + L.v64[0]);
+        double* r64 = reinterpret_cast<double*>(ws + L.v64[1]);
+        float* b32 = reinterpret_cast<float*>(ws + L.v32[0]);
+        float* d32 = reinterpret_cast<float*>(ws + L.v32[1]);
+        float* rr = reinterpret_cast<float*>(ws + L.v32[2]);
+        float* zz = reinterpret_cast<float*>(ws + L.v32[3]);
+        float* pp = reinterpret_cast<float*>(ws + L.v32[4]);
+        float* qq = reinterpret_cast<float*>(ws + L.v32[5]);
+        float* M32 = reinterpret_cast<float*>(ws + L.m32);
+        double* scale = reinterpret_cast<double*>(ws + L.scale);
+        int rc = fem_convert_f64_to_f32(M64, M32, 9 * n, s);
+        if (rc) return rc;
+        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, U);
+        FEM_LAUNCH_CHECK("k_zero");
+        rc = true_residual(U, y, r64);
+        if (rc) return rc;
+        const int max_outer = std::max(1, o->max_outer);
+        double prev = 1e300;
+        for (outer = 0; outer < max_outer; ++outer) {
+            double sc[kMaxR], worst = 0.0;
+            int any = 0;
+            for (int k = 0; k < R; ++k) {
+                const double rn = sqrt(h.norm2[k]);
+                const double rel = bnorm[k] > 0 ? rn / bnorm[k] : 0.0;
+                worst = std::max(worst, rel);
+                const bool act = bnorm[k] > 0 && rel > o->rtol;
+                sc[k] = act ? rn : 0.0;
+                any |= act;
+            }
+            if (!any) break;
+            if (outer > 0 && !(worst < 0.5 * prev)) {
+                status = FEM_ERR_NOT_CONVERGED;  // refinement stalled
+                break;
+            }
+            prev = worst;
+            FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
+            k_scale_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, r64, scale, b32);
+            FEM_LAUNCH_CHECK("k_scale_cast");
+            rc = pcg_core<float, R>(K32, M32, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
+                                    std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll, s, &ir);
+            if (rc) return rc;
+            total_iters += ir.iters;
+            if (ir.status == FEM_ERR_BREAKDOWN || ir.status == FEM_ERR_NOT_SPD) {
+                status = ir.status;
+                break;
+            }
+            k_axpy_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, scale, d32, U);
+            FEM_LAUNCH_CHECK("k_axpy_cast");
+            rc = true_residual(U, y, r64);
+            if (rc) return rc;
+            if (total_iters >= maxit) {
+                status = FEM_ERR_MAXITER;
+                break;
+            }
+        }
+    }
+    double worst = 0.0;
+    for (int k = 0; k < R; ++k) {
+        const double rel = bnorm[k] > 0 ? sqrt(h.norm2[k]) / bnorm[k] : 0.0;
+        worst = std::max(worst, rel);
+    }
+    if (status == FEM_OK && o->mixed && worst > o->rtol) status = FEM_ERR_MAXITER;
+    out->status = status;
+    out->iterations = total_iters;
+    out->outer = outer;
+    out->relres = worst;
+    return FEM_OK;
+}
+
+}  // namespace
+}  // namespace fem
+
+using namespace fem;
+
+extern "C" size_t fem_pcg_workspace_bytes(int64_t n_brow, int nrhs, int mixed) {
+    if (n_brow < 0 || nrhs < 1 || nrhs > kMaxR) return 0;
+    return layout(n_brow, nrhs, mixed ? 1 : 0).total;
+}
+
+extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F,
+                             double* U, const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    FEM_REQUIRE(A64 && opts && stats && precond && F && U, "NULL argument");
+    FEM_REQUIRE(A64->dtype == FEM_F64 && A64->n_brow > 0 && A64->indptr && A64->indices && A64->vals,
+                "A64 must be a non-empty FP64 BSR matrix");
+    const int R = opts->nrhs;
+    FEM_REQUIRE(R == 1 || R == 2 || R == 4 || R == 8 || R == 16 || R == 32, "nrhs must be 1, 2, 4, 8, 16 or 32");
+    FEM_REQUIRE(opts->rtol > 0 && opts->maxit > 0, "rtol and maxit must be positive");
+    if (opts->mixed) {
+        FEM_REQUIRE(A32 && A32->dtype == FEM_F32 && A32->n_brow == A64->n_brow && A32->vals,
+                    "mixed precision needs the FP32 copy of the matrix (A32)");
+        FEM_REQUIRE(opts->inner_rtol > 0 && opts->inner_rtol < 1, "inner_rtol must lie in (0, 1)");
+    }
+    const Layout L = layout(A64->n_brow, R, opts->mixed);
+    if (!workspace || workspace_bytes < L.total) {
+        set_error("workspace too small: need %zu bytes", L.total);
+        return FEM_ERR_WORKSPACE;
+    }
+    FEM_REQUIRE(aligned16(workspace), "workspace must be 16-byte aligned");
+    // Work on a private stream ordered after / before the caller's stream (graph capture
+    // is not allowed on the legacy default stream).
+    cudaStream_t caller = as_stream(stream), s = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, t0 = nullptr, t1 = nullptr;
+    FEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int rc = FEM_OK;
+    auto cleanup = [&]() {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+        if (s) cudaStreamDestroy(s);
+    };
+    do {
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming), "event"))) break;
+        if ((rc = cuda_status(cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming), "event"))) break;
+        if ((rc = cuda_status(cudaEventCreate(&t0), "event"))) break;
+        if ((rc = cuda_status(cudaEventCreate(&t1), "event"))) break;
+        if ((rc = cuda_status(cudaEventRecord(ev0, caller), "record"))) break;
+        if ((rc = cuda_status(cudaStreamWaitEvent(s, ev0, 0), "wait"))) break;
+        if ((rc = cuda_status(cudaEventRecord(t0, s), "record"))) break;
+        unsigned char* ws = static_cast<unsigned char*>(workspace);
+        switch (R) {
+            case 1: rc = solve_r<1>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            case 2: rc = solve_r<2>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            case 4: rc = solve_r<4>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            case 8: rc = solve_r<8>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            case 16: rc = solve_r<16>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            default: rc = solve_r<32>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+        }
+        if (rc) break;
+        if ((rc = cuda_status(cudaEventRecord(t1, s), "record"))) break;
+        if ((rc = cuda_status(cudaEventSynchronize(t1), "sync"))) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, t0, t1);
+        stats->time_ms = ms;
+        if ((rc = cuda_status(cudaEventRecord(ev1, s), "record"))) break;
+        if ((rc = cuda_status(cudaStreamWaitEvent(caller, ev1, 0), "wait"))) break;
+    } while (0);
+    if (rc) cudaStreamSynchronize(s);
+    cleanup();
+    return rc;
+}

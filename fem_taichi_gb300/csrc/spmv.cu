@@ -1,0 +1,202 @@
+// BSR SpMV / SpMM entry points, precision conversion, block-Jacobi inverse and the SpMV
+// launch autotuner.  The kernels are the residual product of SOLVE_static.py:36 (K * U)
+// generalised to FP32 and to many right-hand sides.
+#include <mutex>
+
+#include "spmv.cuh"
+
+namespace fem {
+
+int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
+    return n;
+}
+
+namespace {
+
+template <typename T, int LPR>
+__global__ void __launch_bounds__(512) k_spmv(const BsrView<T> A, const T* __restrict__ x, T* __restrict__ y) {
+    spmv1_rows<T, LPR>(A, x, y, false);
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_spmm(const BsrView<T> A, const T* __restrict__ x, T* __restrict__ y) {
+    spmm_rows<T, R>(A, x, y, false);
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        dst[i] = float(src[i]);
+}
+
+// Inverse of each block row's diagonal block (adjugate / det, FP64).  Rows whose diagonal
+// block is missing or singular get the identity and are counted in *bad.
+__global__ void k_block_jacobi(int64_t n, const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                               const double* __restrict__ vals, double* inv64, float* inv32, int* bad) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t rs = indptr[i], re = indptr[i + 1];
+        int64_t s = -1;
+        for (int64_t k = rs; k < re; ++k)
+            if (indices[k] == int(i)) {
+                s = k;
+                break;
+            }
+        double o[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (s >= 0) {
+            const double* a = vals + 9 * s;
+            double c[9];
+            c[0] = a[4] * a[8] - a[5] * a[7];
+            c[1] = a[2] * a[7] - a[1] * a[8];
+            c[2] = a[1] * a[5] - a[2] * a[4];
+            c[3] = a[5] * a[6] - a[3] * a[8];
+            c[4] = a[0] * a[8] - a[2] * a[6];
+            c[5] = a[2] * a[3] - a[0] * a[5];
+            c[6] = a[3] * a[7] - a[4] * a[6];
+            c[7] = a[1] * a[6] - a[0] * a[7];
+            c[8] = a[0] * a[4] - a[1] * a[3];
+            const double det = a[0] * c[0] + a[1] * c[3] + a[2] * c[6];
+            if (det != 0.0 && isfinite(det)) {
+                const double id = 1.0 / det;
+#pragma unroll
+                for (int k = 0; k < 9; ++k) o[k] = c[k] * id;
+            } else {
+                atomicAdd(bad, 1);
+            }
+        } else {
+            atomicAdd(bad, 1);
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (inv64) inv64[9 * i + k] = o[k];
+            if (inv32) inv32[9 * i + k] = float(o[k]);
+        }
+    }
+}
+
+template <typename T>
+int launch_spmv(const BsrView<T>& A, int nrhs, const T* x, T* y, int variant, cudaStream_t st) {
+    const int sms = sm_count();
+    if (nrhs == 1) {
+        const SpmvVariant v = spmv_variant(variant);
+        const int64_t rows_per_cta = int64_t(v.threads / 32) * (32 / v.lpr);
+        const int64_t need = (A.n + rows_per_cta - 1) / rows_per_cta;
+        const unsigned grid = unsigned(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * v.ctas_per_sm)));
+        switch (v.lpr) {
+            case 32: k_spmv<T, 32><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            case 16: k_spmv<T, 16><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            default: k_spmv<T, 8><<<grid, v.threads, 0, st>>>(A, x, y); break;
+        }
+    } else {
+        const int64_t rows_per_cta = 8 * (32 / nrhs);
+        const int64_t need = (A.n + rows_per_cta - 1) / rows_per_cta;
+        const unsigned grid = unsigned(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * 8)));
+        switch (nrhs) {
+            case 2: k_spmm<T, 2><<<grid, 256, 0, st>>>(A, x, y); break;
+            case 4: k_spmm<T, 4><<<grid, 256, 0, st>>>(A, x, y); break;
+            case 8: k_spmm<T, 8><<<grid, 256, 0, st>>>(A, x, y); break;
+            case 16: k_spmm<T, 16><<<grid, 256, 0, st>>>(A, x, y); break;
+            default: k_spmm<T, 32><<<grid, 256, 0, st>>>(A, x, y); break;
+        }
+    }
+    FEM_LAUNCH_CHECK("bsr spmv");
+    return FEM_OK;
+}
+
+int check_bsr(const fem_bsr* A) {
+    FEM_REQUIRE(A != nullptr, "A is NULL");
+    FEM_REQUIRE(A->n_brow >= 0 && A->nnzb >= 0, "negative size");
+    FEM_REQUIRE(A->dtype == FEM_F64 || A->dtype == FEM_F32, "dtype must be FEM_F64 or FEM_F32");
+    if (A->n_brow) FEM_REQUIRE(A->indptr != nullptr, "indptr is NULL");
+    if (A->nnzb) FEM_REQUIRE(A->indices && A->vals, "indices/vals is NULL");
+    return FEM_OK;
+}
+
+bool valid_nrhs(int r) { return r == 1 || r == 2 || r == 4 || r == 8 || r == 16 || r == 32; }
+
+}  // namespace
+
+int bsr_spmv_any(const fem_bsr* A, int nrhs, const void* x, void* y, int variant, cudaStream_t st) {
+    if (A->n_brow == 0) return FEM_OK;
+    if (A->dtype == FEM_F64) {
+        BsrView<double> v{A->n_brow, A->indptr, A->indices, static_cast<const double*>(A->vals)};
+        return launch_spmv<double>(v, nrhs, static_cast<const double*>(x), static_cast<double*>(y), variant, st);
+    }
+    BsrView<float> v{A->n_brow, A->indptr, A->indices, static_cast<const float*>(A->vals)};
+    return launch_spmv<float>(v, nrhs, static_cast<const float*>(x), static_cast<float*>(y), variant, st);
+}
+
+}  // namespace fem
+
+using namespace fem;
+
+extern "C" int fem_bsr_spmv(const fem_bsr* A, int nrhs, const void* x, void* y, int variant, void* stream) {
+    int rc = check_bsr(A);
+    if (rc) return rc;
+    FEM_REQUIRE(valid_nrhs(nrhs), "nrhs must be 1, 2, 4, 8, 16 or 32");
+    FEM_REQUIRE(A->n_brow == 0 || (x && y), "x/y is NULL");
+    FEM_REQUIRE(x != y || A->n_brow == 0, "x and y must not alias");
+    return bsr_spmv_any(A, nrhs, x, y, variant, as_stream(stream));
+}
+
+extern "C" int fem_convert_f64_to_f32(const double* src, float* dst, int64_t n, void* stream) {
+    FEM_REQUIRE(n >= 0, "negative size");
+    if (n == 0) return FEM_OK;
+    FEM_REQUIRE(src && dst, "src/dst is NULL");
+    const unsigned grid = unsigned(std::min<int64_t>((n + 255) / 256, int64_t(sm_count()) * 16));
+    k_f64_to_f32<<<grid, 256, 0, as_stream(stream)>>>(src, dst, n);
+    FEM_LAUNCH_CHECK("k_f64_to_f32");
+    return FEM_OK;
+}
+
+extern "C" int fem_block_jacobi(const fem_bsr* A, double* inv64, float* inv32, int* n_bad, void* stream) {
+    int rc = check_bsr(A);
+    if (rc) return rc;
+    FEM_REQUIRE(A->dtype == FEM_F64, "block Jacobi needs the FP64 matrix");
+    FEM_REQUIRE(n_bad != nullptr, "n_bad is NULL");
+    if (A->n_brow == 0) return FEM_OK;
+    cudaStream_t st = as_stream(stream);
+    FEM_CUDA(cudaMemsetAsync(n_bad, 0, sizeof(int), st));
+    const unsigned grid = unsigned(std::min<int64_t>((A->n_brow + 255) / 256, int64_t(sm_count()) * 16));
+    k_block_jacobi<<<grid, 256, 0, st>>>(A->n_brow, A->indptr, A->indices, static_cast<const double*>(A->vals),
+                                         inv64, inv32, n_bad);
+    FEM_LAUNCH_CHECK("k_block_jacobi");
+    return FEM_OK;
+}
+
+extern "C" int fem_spmv_autotune(const fem_bsr* A, int nrhs, const void* x, void* y, int reps, int* best_variant,
+                                 float* best_ms, void* stream) {
+    int rc = check_bsr(A);
+    if (rc) return rc;
+    FEM_REQUIRE(valid_nrhs(nrhs) && best_variant, "bad nrhs or best_variant is NULL");
+    FEM_REQUIRE(A->n_brow == 0 || (x && y && x != y), "x/y is NULL or aliased");
+    *best_variant = 0;
+    if (best_ms) *best_ms = 0.f;
+    if (nrhs != 1 || A->n_brow == 0) return FEM_OK;  // SpMM has a single launch shape
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t e0, e1;
+    FEM_CUDA(cudaEventCreate(&e0));
+    FEM_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bid = 0;
+    reps = std::max(1, std::min(reps, 100));
+    for (int v = 0; v < kNumSpmvVariants; ++v) {
+        rc = bsr_spmv_any(A, 1, x, y, v, st);  // warm-up
+        if (rc) break;
+        FEM_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps && rc == FEM_OK; ++r) rc = bsr_spmv_any(A, 1, x, y, v, st);
+        FEM_CUDA(cudaEventRecord(e1, st));
+        FEM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        FEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= reps;
+        if (ms < best) best = ms, bid = v;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *best_variant = bid;
+    if (best_ms) *best_ms = best;
+    return FEM_OK;
+}

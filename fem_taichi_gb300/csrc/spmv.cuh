@@ -1,0 +1,126 @@
+// BSR (3x3 block) SpMV / SpMM device code shared by spmv.cu and pcg.cu.
+//
+// Vectors with nrhs right-hand sides are stored [n_brow][3][nrhs] (right-hand side
+// fastest), so one block row's inputs/outputs for all RHS are contiguous.
+//  * nrhs == 1: LPR lanes cooperate on one block row (lane = block slot), followed by an
+//    xor-shuffle reduction of the three row sums; 32/LPR rows per warp.
+//  * nrhs  > 1: lanes map to right-hand sides (32/nrhs rows per warp); each block's nine
+//    values are loaded once per row group (broadcast) and applied to all RHS.
+// Rows are visited with a grid-stride loop so the grid can be sized in multiples of the SM
+// count; a fixed grid gives a fixed row -> CTA mapping, hence deterministic partial sums.
+#pragma once
+
+#include "fem_common.cuh"
+
+namespace fem {
+
+template <typename T>
+struct BsrView {
+    int64_t n;              // block rows
+    const int32_t* indptr;  // [n+1]
+    const int32_t* indices; // [nnzb]
+    const T* vals;          // [nnzb][3][3]
+};
+
+// Sum over lanes l' with (l' / G) == (l / G) of a warp split into groups of G lanes.
+template <int G, typename V>
+__device__ __forceinline__ V group_sum(V v) {
+#pragma unroll
+    for (int off = G / 2; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// One pass of y = A x over the rows assigned to this thread; returns sum_rows x_i . y_i
+// for this lane's RHS (valid in the lane that writes the row), for PCG's p.q.
+template <typename T, int LPR>
+__device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
+                                             bool want_dot) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / LPR, sl = lane % LPR;
+    constexpr int RPW = 32 / LPR;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
+        const int64_t row = base + sub;
+        const bool valid = row < A.n;
+        T a0 = 0, a1 = 0, a2 = 0;
+        if (valid) {
+            const int64_t rs = __ldg(A.indptr + row);
+            const int L = __ldg(A.indptr + row + 1) - int(rs);
+            for (int l = sl; l < L; l += LPR) {
+                const int64_t c = __ldg(A.indices + rs + l);
+                const T* v = A.vals + 9 * (rs + l);
+                const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
+                a0 += __ldg(v + 0) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
+                a1 += __ldg(v + 3) * x0 + __ldg(v + 4) * x1 + __ldg(v + 5) * x2;
+                a2 += __ldg(v + 6) * x0 + __ldg(v + 7) * x1 + __ldg(v + 8) * x2;
+            }
+        }
+        a0 = group_sum<LPR>(a0);
+        a1 = group_sum<LPR>(a1);
+        a2 = group_sum<LPR>(a2);
+        if (valid && sl == 0) {
+            y[3 * row] = a0;
+            y[3 * row + 1] = a1;
+            y[3 * row + 2] = a2;
+            if (want_dot)
+                dot += double(x[3 * row]) * double(a0) + double(x[3 * row + 1]) * double(a1) +
+                       double(x[3 * row + 2]) * double(a2);
+        }
+    }
+    return dot;
+}
+
+template <typename T, int R>
+__device__ __forceinline__ double spmm_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
+                                            bool want_dot) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / R, rhs = lane % R;
+    constexpr int RPW = 32 / R;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
+        const int64_t row = base + sub;
+        if (row >= A.n) continue;
+        const int64_t rs = __ldg(A.indptr + row);
+        const int L = __ldg(A.indptr + row + 1) - int(rs);
+        T a0 = 0, a1 = 0, a2 = 0;
+        for (int l = 0; l < L; ++l) {
+            const int64_t c = __ldg(A.indices + rs + l);
+            const T* v = A.vals + 9 * (rs + l);
+            const T* xc = x + 3 * c * R + rhs;
+            const T x0 = xc[0], x1 = xc[R], x2 = xc[2 * R];
+            a0 += __ldg(v + 0) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
+            a1 += __ldg(v + 3) * x0 + __ldg(v + 4) * x1 + __ldg(v + 5) * x2;
+            a2 += __ldg(v + 6) * x0 + __ldg(v + 7) * x1 + __ldg(v + 8) * x2;
+        }
+        T* yr = y + 3 * row * R + rhs;
+        yr[0] = a0;
+        yr[R] = a1;
+        yr[2 * R] = a2;
+        if (want_dot) {
+            const T* xr = x + 3 * row * R + rhs;
+            dot += double(xr[0]) * double(a0) + double(xr[R]) * double(a1) + double(xr[2 * R]) * double(a2);
+        }
+    }
+    return dot;
+}
+
+// SpMV launch variants picked by the autotuner (nrhs == 1): lanes per block row and CTA size.
+struct SpmvVariant {
+    int lpr;      // 32, 16 or 8 lanes per block row
+    int threads;  // CTA size
+    int ctas_per_sm;
+};
+constexpr int kNumSpmvVariants = 6;
+__host__ __device__ inline SpmvVariant spmv_variant(int id) {
+    const SpmvVariant v[kNumSpmvVariants] = {{32, 256, 8}, {16, 256, 8}, {8, 256, 8},
+                                             {32, 512, 4}, {16, 128, 16}, {8, 512, 4}};
+    return v[(id >= 0 && id < kNumSpmvVariants) ? id : 0];
+}
+
+int sm_count();
+
+}  // namespace fem

@@ -1,0 +1,201 @@
+"""GPU static solve: drop-in for ``SOLVE_static.Static_solver`` (SOLVE_static.py:6-77).
+
+The reference factorises K with MKL Pardiso (``pardisoSolver(KL, mtype=2)``,
+SOLVE_static.py:31-33).  Here K stays in HBM as 3x3-block BSR and the system is solved by
+the block-preconditioned CG of ``libfemgb.so`` (``fem_pcg_solve``):
+
+* ``mixed=False``: FP64 PCG with block-Jacobi (inverse 3x3 diagonal blocks);
+* ``mixed=True``: FP32 SpMV / FP32 preconditioner inner PCG inside FP64 iterative
+  refinement (true residual r = F - K u in FP64);
+* up to 32 right-hand sides in one solve (lockstep PCG, BSR SpMM);
+* iterations replayed as CUDA graphs; SpMV launch shape chosen by the autotuner.
+
+``Static_solver(Model, Qtype=0).Solve_cpu(max_errs, max_iters)`` keeps the reference's
+signature and return value (U, (3N,) float64) but runs the GPU solve to a tight tolerance
+(there is no CPU path).  ``Solve_gpu(...)`` exposes the options.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import FemBsr, FemPcgOpts, FemPcgStats, FEM_F32, FEM_F64
+from .model import _dptr, _stream
+
+SUPPORTED_NRHS = (1, 2, 4, 8, 16, 32)
+
+_STATUS = {0: "converged", _lib.FEM_ERR_MAXITER: "max iterations", _lib.FEM_ERR_NOT_CONVERGED: "stalled",
+           _lib.FEM_ERR_NOT_SPD: "non-positive curvature", _lib.FEM_ERR_BREAKDOWN: "NaN/Inf breakdown"}
+
+
+def padded_nrhs(r: int) -> int:
+    for s in SUPPORTED_NRHS:
+        if r <= s:
+            return s
+    raise ValueError("at most 32 right-hand sides per solve")
+
+
+class DeviceSystem:
+    """K (FP64 BSR, and its FP32 copy on demand) plus F of a ``Model`` on the device."""
+
+    def __init__(self, model, K=None, F=None):
+        self.model = model
+        self.lib = _lib.load()
+        self.device = model.device
+        if K is None or F is None:
+            K, _, F = model.assemble(K=True, M=False, F=True, k_layout="bsr")
+        self.K64 = K
+        self.F = F.reshape(-1)
+        self.n = model.Num_Node
+        self.nnzb = model.mesh.nnzb
+        self.A64 = FemBsr(self.n, self.nnzb, model.mesh.indptr.data_ptr(), model.mesh.indices.data_ptr(),
+                          self.K64.data_ptr(), FEM_F64)
+        self._K32 = None
+        self._A32 = None
+        self._bj = None
+        self._variant = {}
+        self._ws = None
+
+    @property
+    def stream(self):
+        return _stream(self.device)
+
+    def K32(self):
+        if self._K32 is None:
+            self._K32 = torch.empty(self.K64.shape, dtype=torch.float32, device=self.device)
+            _lib.check(self.lib.fem_convert_f64_to_f32(_dptr(self.K64), _dptr(self._K32), self.K64.numel(),
+                                                       self.stream), "fem_convert_f64_to_f32")
+            self._A32 = FemBsr(self.n, self.nnzb, self.model.mesh.indptr.data_ptr(),
+                               self.model.mesh.indices.data_ptr(), self._K32.data_ptr(), FEM_F32)
+        return self._K32
+
+    def block_jacobi(self) -> torch.Tensor:
+        """(N, 9) FP64 inverses of the diagonal blocks."""
+        if self._bj is None:
+            bj = torch.empty((self.n, 9), dtype=torch.float64, device=self.device)
+            bad = torch.zeros(1, dtype=torch.int32, device=self.device)
+            _lib.check(self.lib.fem_block_jacobi(ctypes.byref(self.A64), _dptr(bj), None, _dptr(bad), self.stream),
+                       "fem_block_jacobi")
+            if int(bad.item()):
+                raise _lib.FemError(_lib.FEM_ERR_NOT_SPD, f"{int(bad.item())} singular diagonal blocks")
+            self._bj = bj
+        return self._bj
+
+    def spmv(self, x: torch.Tensor, fp32=False, nrhs=1) -> torch.Tensor:
+        A = self._A32 if fp32 else self.A64
+        if fp32:
+            self.K32()
+            A = self._A32
+        y = torch.empty_like(x)
+        _lib.check(self.lib.fem_bsr_spmv(ctypes.byref(A), nrhs, _dptr(x), _dptr(y),
+                                         self.variant(fp32, nrhs), self.stream), "fem_bsr_spmv")
+        return y
+
+    def variant(self, fp32: bool, nrhs: int) -> int:
+        """Autotuned SpMV launch variant for (precision, nrhs), tuned once on this matrix."""
+        key = (fp32, nrhs)
+        if key not in self._variant:
+            if nrhs != 1:
+                self._variant[key] = 0
+            else:
+                if fp32:
+                    self.K32()
+                A = self._A32 if fp32 else self.A64
+                dt = torch.float32 if fp32 else torch.float64
+                x = torch.ones(3 * self.n, dtype=dt, device=self.device)
+                y = torch.empty_like(x)
+                best = ctypes.c_int(0)
+                ms = ctypes.c_float(0)
+                _lib.check(self.lib.fem_spmv_autotune(ctypes.byref(A), 1, _dptr(x), _dptr(y), 5, ctypes.byref(best),
+                                                      ctypes.byref(ms), self.stream), "fem_spmv_autotune")
+                self._variant[key] = best.value
+        return self._variant[key]
+
+    def solve(self, F=None, rtol=1e-10, maxit=50000, mixed=True, precond=None, use_graph=True, unroll=16,
+              inner_rtol=1e-4, inner_maxit=20000, max_outer=40):
+        """Solve K U = F.  F: device/host array (3N,) or (3N, R) (default: the assembled F).
+
+        precond: (N, 9) FP64 blocks (default block Jacobi).  Returns (U (3N,) or (3N, R)
+        device tensor, stats dict)."""
+        if F is None:
+            F = self.F
+        F = torch.as_tensor(F, dtype=torch.float64, device=self.device)
+        squeeze = F.dim() == 1
+        F2 = F.reshape(3 * self.n, -1)
+        R = F2.shape[1]
+        Rp = padded_nrhs(R)
+        if Rp != R:
+            F2 = torch.cat([F2, torch.zeros((3 * self.n, Rp - R), dtype=torch.float64, device=self.device)], 1)
+        F2 = F2.contiguous()
+        U = torch.empty_like(F2)
+        P = self.block_jacobi() if precond is None else torch.as_tensor(precond, dtype=torch.float64,
+                                                                         device=self.device).reshape(self.n, 9)
+        P = P.contiguous()
+        if mixed:
+            self.K32()
+        nbytes = int(self.lib.fem_pcg_workspace_bytes(self.n, Rp, int(mixed)))
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        opts = FemPcgOpts(Rp, int(mixed), float(rtol), int(maxit), float(inner_rtol), int(inner_maxit),
+                          int(max_outer), int(use_graph), int(unroll), self.variant(False, Rp),
+                          self.variant(True, Rp) if mixed else 0)
+        st = FemPcgStats()
+        A32 = ctypes.byref(self._A32) if mixed else None
+        _lib.check(self.lib.fem_pcg_solve(ctypes.byref(self.A64), A32, _dptr(P), _dptr(F2), _dptr(U),
+                                          ctypes.byref(opts), ctypes.byref(st), _dptr(self._ws), self._ws.numel(),
+                                          self.stream), "fem_pcg_solve")
+        stats = {"status": st.status, "status_text": _STATUS.get(st.status, str(st.status)),
+                 "iterations": st.iterations, "outer": st.outer, "relres": st.relres, "time_ms": st.time_ms,
+                 "nrhs": R, "mixed": bool(mixed)}
+        U = U[:, :R]
+        return (U.reshape(-1) if squeeze else U), stats
+
+
+class Static_solver:
+    """Drop-in for SOLVE_static.Static_solver (linear part, Qtype=0)."""
+
+    def __init__(self, Model, Qtype=0):
+        self.Qtype = Qtype
+        self.Model = Model
+        self.system = None
+        self.last_stats = None
+
+    def _system(self):
+        if self.system is None:
+            self.system = DeviceSystem(self.Model)
+        return self.system
+
+    def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, **kw):
+        """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'learned' (uses
+        ``self.Model.learned_precond`` (N, 9) if set, falling back to block Jacobi when the
+        learned solve does not converge) or an (N, 9) array."""
+        if self.Qtype != 0:
+            raise NotImplementedError("large-displacement Newton solve (SOLVE_static.py:41-75) is not built")
+        S = self._system()
+        P = None
+        fallback = False
+        if isinstance(precond, str):
+            if precond == "learned":
+                P = getattr(self.Model, "learned_precond", None)
+                if P is None:
+                    raise ValueError("no learned preconditioner attached to the model (Model.learned_precond)")
+                fallback = True
+            elif precond != "bj":
+                raise ValueError("precond must be 'bj', 'learned' or an (N, 9) array")
+        else:
+            P = precond
+        U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P, **kw)
+        if fallback and st["status"] != 0:
+            U, st2 = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=None, **kw)
+            st2["fallback_from"] = st
+            st = st2
+        self.last_stats = st
+        return U.cpu().numpy()
+
+    def Solve_cpu(self, max_errs=1e-4, max_iters=20):
+        """SOLVE_static.py:12-39 signature (Qtype 0): returns U (3N,).  Runs the GPU solve
+        to a relative residual of 1e-12 (the reference used a direct factorisation)."""
+        return self.Solve_gpu(rtol=1e-12, mixed=True)

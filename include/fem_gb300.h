@@ -120,6 +120,64 @@ int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
                const int32_t* co_elem, const double* extrap, double* out, void* workspace,
                size_t workspace_bytes, void* stream);
 
+/* ---- BSR operators and the static solve ------------------------------------------- */
+#define FEM_F64 0
+#define FEM_F32 1
+
+typedef struct fem_bsr {
+    int64_t n_brow, nnzb;   /* block rows (= nodes), 3x3 blocks                         */
+    const int32_t* indptr;  /* [n_brow+1]                                               */
+    const int32_t* indices; /* [nnzb]                                                   */
+    const void* vals;       /* [nnzb][3][3] double (FEM_F64) or float (FEM_F32)         */
+    int dtype;
+} fem_bsr;
+
+/* y = A x (SOLVE_static.py:36, KL * U).  nrhs in {1,2,4,8,16,32}; x, y: [n_brow][3][nrhs]
+ * in A's precision.  variant: launch shape from fem_spmv_autotune (0 = default). */
+int fem_bsr_spmv(const fem_bsr* A, int nrhs, const void* x, void* y, int variant, void* stream);
+/* Times every nrhs == 1 launch variant on A (reps launches each) and returns the fastest.
+ * No reference counterpart (tuning of the block-row tile shape). */
+int fem_spmv_autotune(const fem_bsr* A, int nrhs, const void* x, void* y, int reps, int* best_variant,
+                      float* best_ms, void* stream);
+/* dst[i] = (float)src[i]: the FP32 copy of K / of preconditioner blocks for the mixed solve. */
+int fem_convert_f64_to_f32(const double* src, float* dst, int64_t n, void* stream);
+/* Inverses of the 3x3 diagonal blocks (block-Jacobi preconditioner), FP64 and/or FP32
+ * outputs [n_brow][9] (either may be NULL); *n_bad (device int) counts rows whose diagonal
+ * block is missing or singular (identity used). */
+int fem_block_jacobi(const fem_bsr* A, double* inv64, float* inv32, int* n_bad, void* stream);
+
+typedef struct fem_pcg_opts {
+    int nrhs;           /* 1, 2, 4, 8, 16 or 32 right-hand sides solved in lockstep          */
+    int mixed;          /* 0: FP64 PCG; 1: FP32 inner PCG + FP64 iterative refinement       */
+    double rtol;        /* stop when ||F - K U|| / ||F|| <= rtol for every RHS              */
+    int maxit;          /* cap on PCG iterations (total inner iterations when mixed)         */
+    double inner_rtol;  /* mixed: relative residual reduction asked of each inner FP32 solve */
+    int inner_maxit;    /* mixed: cap per inner solve                                        */
+    int max_outer;      /* mixed: cap on refinement steps                                    */
+    int use_graph;      /* replay `unroll` iterations as one CUDA graph                      */
+    int unroll;         /* iterations per graph / per host convergence check                 */
+    int spmv_variant;   /* launch variant of the FP64 SpMV (fem_spmv_autotune)               */
+    int spmv_variant32; /* launch variant of the FP32 SpMV                                   */
+} fem_pcg_opts;
+
+typedef struct fem_pcg_stats {
+    int status;        /* FEM_OK, FEM_ERR_MAXITER, FEM_ERR_NOT_CONVERGED, FEM_ERR_NOT_SPD, ... */
+    int iterations;    /* PCG iterations executed (sum of inner iterations when mixed)        */
+    int outer;         /* refinement steps (1 for FP64 PCG)                                   */
+    double relres;     /* max over RHS of the FP64 true residual ||F - K U|| / ||F||          */
+    double time_ms;    /* device time of the solve (CUDA events)                              */
+} fem_pcg_stats;
+
+/* Solve K U = F (SOLVE_static.py:31-33; Pardiso replaced by PCG).  precond: [n_brow][9]
+ * FP64 preconditioner blocks applied as z_i = P_i r_i (block Jacobi from fem_block_jacobi,
+ * or a learned SPD correction).  F, U: [n_brow][3][nrhs] FP64.  A32 (FP32 copy of A64) is
+ * required when opts->mixed.  The call returns FEM_OK when it ran; stats->status tells
+ * whether the tolerance was met. */
+size_t fem_pcg_workspace_bytes(int64_t n_brow, int nrhs, int mixed);
+int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F, double* U,
+                  const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------ */
 /* Measured FP64 FMA throughput of this device (TFLOP/s, 2 flops per FMA), from a kernel of
  * independent fma chains timed with CUDA events on `stream`.  No reference counterpart: it
