@@ -77,11 +77,34 @@ __device__ bool block_partials(const double (&v)[NS], double* part, unsigned* ti
     return last;
 }
 
-// In the last CTA: total over CTAs (in CTA order) of slot s for RHS k.
-__device__ __forceinline__ double total(const double* part, int nblocks, int s, int k) {
-    double acc = 0.0;
-    for (int b = 0; b < nblocks; ++b) acc += __ldcg(part + (int64_t(b) * kSlots + s) * kMaxR + k);
-    return acc;
+// In the last CTA (all threads call it): tot[s][k] = sum over CTAs of slot s, RHS k.  The
+// kThreads / R threads of each RHS stride over the CTAs, then a fixed-shape tree in shared
+// memory combines them, so the result does not depend on timing.
+template <int R, int NS>
+__device__ void last_block_totals(const double* part, int nblocks, double (&tot)[NS][kMaxR]) {
+    constexpr int G = kThreads / R;
+    __shared__ double red[NS][kThreads];
+    const int t = threadIdx.x, k = t % R, g = t / R;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        double acc = 0.0;
+        for (int b = g; b < nblocks; b += G) acc += __ldcg(part + (int64_t(b) * kSlots + s) * kMaxR + k);
+        red[s][t] = acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int off = G / 2; off >= 1; off >>= 1) {
+        if (g < off) {
+#pragma unroll
+            for (int s = 0; s < NS; ++s) red[s][t] += red[s][t + off * R];
+        }
+        __syncthreads();
+    }
+    if (t < R) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) tot[s][t] = red[s][t];
+    }
+    __syncthreads();
 }
 
 // z = M r for one node / RHS, M the node's 3x3 preconditioner block.
@@ -121,13 +144,16 @@ __global__ void __launch_bounds__(kThreads) k_init(int64_t n, const T* __restric
             v[1] += double(r0) * double(r0) + double(r1) * double(r1) + double(r2) * double(r2);
         }
     }
-    if (block_partials<R, 2>(v, part, &st->ticket) && threadIdx.x == 0) {
+    if (!block_partials<R, 2>(v, part, &st->ticket)) return;
+    __shared__ double tot[2][kMaxR];
+    last_block_totals<R, 2>(part, gridDim.x, tot);
+    if (threadIdx.x == 0) {
         int any = 0, status = FEM_OK;
         for (int k = 0; k < kMaxR; ++k) {
             double rz = 0.0, rr = 0.0;
             if (k < R) {
-                rz = total(part, gridDim.x, 0, k);
-                rr = total(part, gridDim.x, 1, k);
+                rz = tot[0][k];
+                rr = tot[1][k];
             }
             const bool finite = isfinite(rz) && isfinite(rr);
             if (!finite) status = FEM_ERR_BREAKDOWN;
@@ -171,16 +197,21 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pq(const BsrView<T> A, const 
         v[0] = spmv1_rows<T, LPR_OR_R>(A, p, q, true);
     else
         v[0] = spmm_rows<T, LPR_OR_R>(A, p, q, true);
+    constexpr int RR = LPR_OR_R;
+    __shared__ double tot[1][kMaxR];
     bool last;
-    if (R == 1)
+    if (R == 1) {
         last = block_partials<1, 1>(v, part, &st->ticket);
-    else
-        last = block_partials<LPR_OR_R, 1>(v, part, &st->ticket);
+        if (last) last_block_totals<1, 1>(part, gridDim.x, tot);
+    } else {
+        last = block_partials<RR, 1>(v, part, &st->ticket);
+        if (last) last_block_totals<RR, 1>(part, gridDim.x, tot);
+    }
     if (last) {
         const int k = threadIdx.x;
         if (k < R) {
             if (st->active[k]) {
-                const double pq = total(part, gridDim.x, 0, k);
+                const double pq = tot[0][k];
                 st->pq[k] = pq;
                 if (pq > 0.0 && isfinite(pq)) {
                     st->alpha[k] = st->rz[k] / pq;
@@ -230,9 +261,11 @@ __global__ void __launch_bounds__(kThreads) k_update(int64_t n, const T* __restr
         }
     }
     if (block_partials<R, 2>(v, part, &st->ticket)) {
+        __shared__ double tot[2][kMaxR];
+        last_block_totals<R, 2>(part, gridDim.x, tot);
         const int k = threadIdx.x;
         if (k < R && st->active[k]) {
-            const double rz = total(part, gridDim.x, 0, k), rr = total(part, gridDim.x, 1, k);
+            const double rz = tot[0][k], rr = tot[1][k];
             st->beta[k] = rz / st->rz[k];
             st->rz[k] = rz;
             st->rr[k] = rr;
@@ -274,7 +307,9 @@ __global__ void __launch_bounds__(kThreads) k_residual(int64_t nv, const double*
         }
     }
     if (block_partials<R, 1>(v, part, &st->ticket)) {
-        if (threadIdx.x < R) st->norm2[threadIdx.x] = total(part, gridDim.x, 0, threadIdx.x);
+        __shared__ double tot[1][kMaxR];
+        last_block_totals<R, 1>(part, gridDim.x, tot);
+        if (threadIdx.x < R) st->norm2[threadIdx.x] = tot[0][threadIdx.x];
         __syncthreads();
         if (threadIdx.x == 0) st->ticket = 0;
     }
@@ -442,6 +477,8 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
         FEM_CUDA(cudaStreamSynchronize(s));
         return FEM_OK;
     };
+    // the reduction ticket and all scalars start from zero (the workspace is uninitialised)
+    FEM_CUDA(cudaMemsetAsync(st, 0, sizeof(PcgState), s));
     double bnorm[kMaxR];
     {
         // ||F_k||: residual of u = 0
