@@ -75,6 +75,11 @@ class FemPcgStats(ctypes.Structure):
                 ("time_ms", c_double)]
 
 
+class FemMlp(ctypes.Structure):
+    _fields_ = [("W1", c_void_p), ("b1", c_void_p), ("W2", c_void_p), ("b2", c_void_p), ("W3", c_void_p),
+                ("b3", c_void_p)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/fem_gb300.h
 SIGNATURES = {
     "fem_last_error": (ctypes.c_char_p, []),
@@ -99,6 +104,22 @@ SIGNATURES = {
     "fem_pcg_workspace_bytes": (c_size_t, [c_int64, c_int, c_int]),
     "fem_pcg_solve": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,
                               ctypes.POINTER(FemPcgOpts), ctypes.POINTER(FemPcgStats), c_void_p, c_size_t, c_void_p]),
+    "fem_mlp_nparams": (c_int, []),
+    "fem_precond_cholesky": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p]),
+    "fem_precond_features": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p]),
+    "fem_probe_products": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p]),
+    "fem_mlp_forward": (c_int, [ctypes.POINTER(FemMlp), c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
+    "fem_mlp_loss_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p, c_void_p,
+                                  ctypes.POINTER(c_int), c_void_p]),
+    "fem_mlp_backward_workspace_bytes": (c_size_t, [c_int64]),
+    "fem_mlp_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                 c_size_t, c_void_p]),
+    "fem_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_learned_blocks": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_stress_workspace_bytes": (c_size_t, [c_int64]),
     "fem_stress": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

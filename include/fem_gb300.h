@@ -178,6 +178,46 @@ int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond,
                   const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
                   void* stream);
 
+/* ---- learned block-Jacobi correction (no reference counterpart) ------------------ */
+/* Per-node MLP 16 -> 64 -> 64 -> 6 (SiLU), BF16 weights in PyTorch [out][in] layout, FP32
+ * biases.  Output o (6 used of 16) gives L = [[e^o0,0,0],[o3,e^o1,0],[o4,o5,e^o2]] and the
+ * preconditioner block P_i = G_i^{-T} L L^T G_i^{-1}, D_i = G_i G_i^T the diagonal block. */
+typedef struct fem_mlp {
+    const uint16_t* W1; /* [64][16] bf16 */
+    const float* b1;    /* [64] */
+    const uint16_t* W2; /* [64][64] bf16 */
+    const float* b2;    /* [64] */
+    const uint16_t* W3; /* [16][64] bf16, rows 6..15 zero */
+    const float* b3;    /* [16] */
+} fem_mlp;
+
+int fem_mlp_nparams(void); /* flat FP32 parameter vector: W1, b1, W2, b2, W3, b3 */
+/* ginv[n][9] = inverse Cholesky factors of the diagonal blocks of A (FP64 BSR). */
+int fem_precond_cholesky(const fem_bsr* A, double* ginv, int* n_bad, void* stream);
+/* Node features X[n][16] (bf16; Xf optional FP32 copy); lo/hi: HOST bounding box. */
+int fem_precond_features(const fem_bsr* A, const double* ginv, const double* xyz, const uint8_t* fixed,
+                         const double* lo, const double* hi, uint16_t* X, float* Xf, void* stream);
+/* Probe products yhat = G^{-1} K G^{-T} z for nrhs probes ([n][3][nrhs]); w, y: FP64 scratch. */
+int fem_probe_products(const fem_bsr* A, int nrhs, const double* ginv, const double* z, double* w, double* y,
+                       float* yhat, void* stream);
+/* Fused forward pass on the tensor cores (tcgen05); out[n][16]; z1, z2 ([n][64]
+ * pre-activations, optional) for training; *err (device int) set if a wait timed out. */
+int fem_mlp_forward(const fem_mlp* net, const uint16_t* X, int64_t n, float* out, float* z1, float* z2, int* err,
+                    void* stream);
+/* Loss mean_{i,r} |C_i yhat_ir - zhat_ir|^2 (as per-CTA partials, *n_partials of them, to be
+ * summed and scaled by 1/(n nprobe)) and its gradient dout[n][16]. */
+int fem_mlp_loss_grad(const float* out, const float* yhat, const float* zhat, int nprobe, int64_t n, float* dout,
+                      double* loss_partials, int* n_partials, void* stream);
+size_t fem_mlp_backward_workspace_bytes(int64_t n);
+/* Parameter gradient grad[nparams] (deterministic CTA-ordered reduction). */
+int fem_mlp_backward(const float* params, const uint16_t* X, const float* z1, const float* z2, const float* dout,
+                     int64_t n, float* grad, void* workspace, size_t workspace_bytes, void* stream);
+/* Adam step on the FP32 parameters (step >= 1); refreshes the BF16 weight copies. */
+int fem_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1, float beta2,
+                 float eps, uint16_t* W1, uint16_t* W2, uint16_t* W3, void* stream);
+/* P[n][9] = G^{-T} C G^{-1} (FP64) from the MLP outputs. */
+int fem_learned_blocks(int64_t n, const float* out, const double* ginv, double* P, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------ */
 /* Measured FP64 FMA throughput of this device (TFLOP/s, 2 flops per FMA), from a kernel of
  * independent fma chains timed with CUDA events on `stream`.  No reference counterpart: it
