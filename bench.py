@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-solve", action="store_true", help="skip the c3/c4 static-solve studies")
+    ap.add_argument("--c5", action="store_true", help="add the capped 32-RHS twisted-slab study")
     return ap.parse_args()
 
 
@@ -369,6 +371,24 @@ def main():
                           "frac_hbm": sbytes / (sms * 1e-3) / 1e9 / peak, "Mnodes_per_s": N / sms / 1e3}
         line["stress"]["gpu_launches"] = 2 * ns
         line["host_setup_s"] = {"mesh_and_pattern": t_mesh}
+
+    # -- static solve studies (seconds to 1e-8 relative error vs an FP64 reference) ---------------
+    if not a.no_solve and rank == 0:
+        from fem_taichi_gb300 import study
+
+        def brief(r):
+            keep = ("label", "wall_s", "iterations", "outer", "relres", "relerr", "meets_1e-8", "status_text")
+            return {"reference": r["reference"], "solves": [{k: x[k] for k in keep} for x in r["solves"]]}
+
+        sol = {"c3": brief(study.c3_study(device=dev))}
+        r4, net = study.c4_study(device=dev)
+        sol["c4"] = brief(r4)
+        sol["c4"]["training"] = r4["training"]
+        sol["c4"]["inference_s"] = r4["inference_s"]
+        if a.c5:
+            r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=3000)
+            sol["c5"] = brief(r5)
+        line["solve"] = sol
 
     # -- CPU baseline (rank 0, N = 1) -----------------------------------------------------------
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:

@@ -1,0 +1,184 @@
+"""Solve studies on the synthetic workloads (used by bench.py).
+
+* ``c3``: 100x100x20 block stretched 4:1 in z, bottom fixed, uniform top traction: FP64
+  block-Jacobi PCG vs FP32-inner / FP64-refinement PCG to a relative residual of 1e-10.
+* ``c4``: learned preconditioner.  Training set: 50 jittered blocks whose element counts
+  are drawn uniformly to give 20k-200k nodes, element aspect ratio (z stretch) uniform in
+  [1, 8], EX uniform in [7e4, 2.1e5], PO uniform in [0.25, 0.35]; probes z ~ N(0, I).
+  Evaluation: the unseen 160x160x20 block.
+* ``c5``: 1200x120x15 slab over 1000x60x8 mm twisted 60 degrees, root fixed, 32
+  right-hand sides (centrifugal load + 31 seeded random tip-face nodal tractions).
+
+Every solution is compared with an FP64 reference solve of the same system (FP32-inner /
+FP64-refinement PCG driven to a relative residual of 1e-13; its own error is estimated by a
+second solve at 1e-12), standing in for the reference's MKL Pardiso.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import torch
+
+from . import mesh as _mesh
+from .learned import LearnedPreconditioner, NodeData
+from .model import Model
+from .solve import DeviceSystem
+
+STEEL = _mesh.STEEL
+
+
+def training_meshes(count=50, seed=0, min_nodes=20_000, max_nodes=200_000):
+    """Seeded training blocks (see module docstring); yields (Physics, Materials)."""
+    rng = np.random.default_rng(seed)
+    for k in range(count):
+        target = rng.uniform(min_nodes, max_nodes)
+        aspect = rng.uniform(1.0, 8.0)
+        mat = {'DE': 7.8e-9, 'EX': float(rng.uniform(7e4, 2.1e5)), 'PO': float(rng.uniform(0.25, 0.35))}
+        nz = max(4, int(round((target / 16.0) ** (1.0 / 3.0))))
+        nx = max(4, int(round(np.sqrt(target / (nz + 1)) - 1)))
+        ny = max(4, int(round(target / ((nx + 1) * (nz + 1)) - 1)))
+        P = _mesh.hex_block(nx, ny, nz, size=(float(nx), float(ny), float(nz) * aspect), jitter=0.1,
+                            seed=1000 * seed + k, fix="zmin", name=f"train{k}")
+        yield P, mat
+
+
+def concat(datasets):
+    """One NodeData-like batch from many (features and probe pairs are per node)."""
+    class Batch:
+        pass
+    b = Batch()
+    b.X = torch.cat([d.X for d in datasets])
+    b.yhat = torch.cat([d.yhat for d in datasets])
+    b.zhat = torch.cat([d.zhat for d in datasets])
+    b.n = int(b.X.shape[0])
+    b.R = datasets[0].R
+    return b
+
+
+def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda"):
+    t0 = time.perf_counter()
+    data = []
+    nodes = 0
+    for P, mat in training_meshes(count, seed):
+        S = DeviceSystem(Model(P.name, P, mat, device=device))
+        data.append(NodeData(S, n_probes=n_probes, seed=len(data)))
+        nodes += P.Num_Node
+        del S
+    batch = concat(data)
+    del data
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = LearnedPreconditioner(device=device, seed=seed)
+    l0 = net.evaluate_loss([batch])
+    t1 = time.perf_counter()
+    hist = net.train([batch], steps=steps, lr=lr)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    return net, {"meshes": count, "nodes": nodes, "probes": n_probes, "steps": steps, "loss_start": l0,
+                 "loss_end": hist[-1], "data_s": t_data, "train_s": t_train}
+
+
+def reference_solution(S: DeviceSystem, F=None):
+    """FP64 reference (refinement to 1e-13) and its estimated relative error."""
+    U1, s1 = S.solve(F=F, rtol=1e-13, mixed=True, maxit=200000, inner_maxit=50000, max_outer=60)
+    U2, s2 = S.solve(F=F, rtol=1e-12, mixed=True, maxit=200000, inner_maxit=50000, max_outer=60)
+    est = float(torch.linalg.norm(U1 - U2) / torch.linalg.norm(U1))
+    return U1, {"relres": s1["relres"], "status": s1["status"], "est_err_of_1e-12_solve": est}
+
+
+def relerr(U, Ur):
+    if U.dim() == 1:
+        return float(torch.linalg.norm(U - Ur) / torch.linalg.norm(Ur))
+    return float(((U - Ur).norm(dim=0) / Ur.norm(dim=0)).max())
+
+
+def timed_solve(S, label, reps=1, **kw):
+    U, st = S.solve(**kw)          # warm (graphs, autotune, FP32 copy)
+    best = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        U, st = S.solve(**kw)
+        torch.cuda.synchronize()
+        w = time.perf_counter() - t
+        best = w if best is None else min(best, w)
+    st = dict(st)
+    st["wall_s"] = best
+    st["label"] = label
+    return U, st
+
+
+def compare(S: DeviceSystem, Ur, variants, F=None, target=1e-8):
+    """Each variant: (label, kwargs).  Adds relative error vs Ur; marks pass at target."""
+    rows = []
+    for label, kw in variants:
+        U, st = timed_solve(S, label, F=F, **kw)
+        st["relerr"] = relerr(U, Ur)
+        st["meets_1e-8"] = bool(st["relerr"] <= target and st["status"] == 0)
+        rows.append(st)
+    return rows
+
+
+def c3_study(device="cuda", rtol=1e-10):
+    P = _mesh.config_mesh("c3")
+    extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
+    S = DeviceSystem(Model("c3", P, STEEL, device=device, extra_loads=extra))
+    Ur, ref = reference_solution(S)
+    rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
+                           ("mixed_bj", dict(rtol=rtol, mixed=True))])
+    return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows}
+
+
+def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
+    info = {}
+    if net is None:
+        net, info = train_c4(device=device, **(train_kw or {}))
+    P = _mesh.config_mesh("c4", fix="zmin", load_face=None)
+    extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
+    M = Model("c4", P, STEEL, device=device, extra_loads=extra)
+    S = DeviceSystem(M)
+    t = time.perf_counter()
+    Pl = net.blocks(S)
+    torch.cuda.synchronize()
+    t_inf = time.perf_counter() - t
+    Ur, ref = reference_solution(S)
+    rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
+                           ("mixed_bj", dict(rtol=rtol, mixed=True)),
+                           ("mixed_learned", dict(rtol=rtol, mixed=True, precond=Pl)),
+                           ("fp64_learned", dict(rtol=rtol, mixed=False, precond=Pl))])
+    return {"workload": "c4 eval 160x160x20, 544,341 nodes", "training": info, "inference_s": t_inf,
+            "reference": ref, "solves": rows}, net
+
+
+def c5_system(device="cuda", nrhs=32, seed=5):
+    P = _mesh.config_mesh("c5")
+    M = Model("c5", P, STEEL, device=device)
+    S = DeviceSystem(M)
+    nx, ny, nz = P.grid
+    ix, iy, iz = P.grid_index
+    tip = np.nonzero(ix == nx)[0]
+    rng = np.random.default_rng(seed)
+    Fm = torch.zeros((3 * P.Num_Node, nrhs), dtype=torch.float64, device=S.device)
+    Fm[:, 0] = S.F
+    for k in range(1, nrhs):
+        f = np.zeros((P.Num_Node, 3))
+        f[tip] = rng.standard_normal((tip.size, 3))
+        Fm[:, k] = torch.from_numpy(f.reshape(-1)).to(S.device)
+    return S, Fm
+
+
+def c5_study(net, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3000):
+    """Capped: block-diagonal preconditioners need far more than ``maxit`` iterations on
+    this slender slab, so the study reports the residual reached within the cap."""
+    S, Fm = c5_system(device, nrhs)
+    Pl = net.blocks(S)
+    U1, s1 = S.solve(F=Fm, rtol=1e-13, mixed=False, maxit=maxit)
+    Ur, ref = U1, {"relres": s1["relres"], "status": s1["status"], "note": f"FP64 PCG capped at {maxit}"}
+    variants = [("mixed_learned", dict(rtol=rtol, mixed=True, precond=Pl, maxit=maxit, inner_maxit=maxit)),
+                ("mixed_bj", dict(rtol=rtol, mixed=True, maxit=maxit, inner_maxit=maxit))]
+    if include_fp64:
+        variants.append(("fp64_bj", dict(rtol=rtol, mixed=False, maxit=maxit)))
+    rows = compare(S, Ur, variants, F=Fm)
+    return {"workload": f"c5 twisted slab 1200x120x15, 2,325,136 nodes, {nrhs} RHS", "reference": ref,
+            "solves": rows}
