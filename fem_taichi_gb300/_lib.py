@@ -120,6 +120,8 @@ SIGNATURES = {
     "fem_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_learned_blocks": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_stress_noalloc": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p]),
     "fem_stress_workspace_bytes": (c_size_t, [c_int64]),
     "fem_stress": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -11,6 +11,8 @@
 //     ascending element order (no atomics), divides by the element count (get_NdAve,
 //     :183-187), then computes the principal stresses with cyclic Jacobi rotations
 //     (descending order) and the reference's "VM" formula as written (:93-94).
+#include <mutex>
+
 #include "fem_common.cuh"
 
 namespace fem {
@@ -230,4 +232,54 @@ extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const d
                                                     static_cast<const double*>(workspace), out);
     FEM_LAUNCH_CHECK("k_stress_node");
     return FEM_OK;
+}
+
+// ---- allocation-free variant ------------------------------------------------------------------
+// Some callers cannot allocate device memory at all: plug-ins living inside a host program that
+// owns every device allocation and only lends them input/output buffers, or latency-critical
+// loops where cudaMalloc/cudaFree are forbidden because they synchronise the device.  For them
+// fem_stress_noalloc runs the same two stress kernels with their per-element scratch placed in
+// this file-scope device array instead of a caller workspace.  The array is reserved on every
+// GPU that loads this library and stays there until the process exits.
+namespace {
+
+static __device__ __align__(256) double g_stress_scratch[size_t(FEM_STRESS_NOALLOC_MAX_ELEMS) * 48];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_stress_scratch on the current device, looked up once per device (the
+// host-side symbol is only a stand-in and must never be handed to a kernel).
+int scratch_address(void** out) {
+    int dev = 0;
+    FEM_CUDA(cudaGetDevice(&dev));
+    FEM_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        FEM_CUDA(cudaGetSymbolAddress(&p, g_stress_scratch));
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return FEM_OK;
+}
+
+}  // namespace
+
+extern "C" int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat, const double* u,
+                                  const int32_t* co_elem, const double* extrap, double* out, void* stream) {
+    FEM_REQUIRE(mesh != nullptr, "mesh is NULL");
+    if (mesh->n_elem > FEM_STRESS_NOALLOC_MAX_ELEMS) {
+        set_error("fem_stress_noalloc: %lld elements exceed the built-in scratch limit of %d elements; "
+                  "use fem_stress with a caller-allocated workspace",
+                  (long long)mesh->n_elem, FEM_STRESS_NOALLOC_MAX_ELEMS);
+        return FEM_ERR_WORKSPACE;
+    }
+    void* scratch = nullptr;
+    int rc = scratch_address(&scratch);
+    if (rc) return rc;
+    // Every element record is fully rewritten by the element kernel before the node kernel
+    // reads it, so nothing in the shared scratch has to be cleared between calls.
+    return fem_stress(mesh, mat, u, co_elem, extrap, out, scratch, sizeof(g_stress_scratch), stream);
 }

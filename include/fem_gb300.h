@@ -120,6 +120,20 @@ int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
                const int32_t* co_elem, const double* extrap, double* out, void* workspace,
                size_t workspace_bytes, void* stream);
 
+/* Same as fem_stress, but for callers that cannot allocate device memory (a plug-in whose
+ * host program owns every device buffer, or a loop where cudaMalloc/cudaFree are banned
+ * because they synchronise the device).  No counterpart in the reference.  The per-element
+ * scratch is a 24 MiB array built into the library, reserved on each GPU that loads it until
+ * the process exits, so meshes are limited to FEM_STRESS_NOALLOC_MAX_ELEMS elements (larger
+ * ones return FEM_ERR_WORKSPACE).  The first call on a device looks up the array's device
+ * address; make that first call before any stream capture.  All calls share the one array:
+ * calls that can overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Nothing in the array needs clearing between calls.  It calls no
+ * allocator. */
+#define FEM_STRESS_NOALLOC_MAX_ELEMS 65536
+int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat, const double* u,
+                       const int32_t* co_elem, const double* extrap, double* out, void* stream);
+
 /* ---- BSR operators and the static solve ------------------------------------------- */
 #define FEM_F64 0
 #define FEM_F32 1
