@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
+    ap.add_argument("--algo", choices=["dd", "fp64"], default="dd", help="assembly arithmetic")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -237,8 +238,9 @@ def main():
     Mt = torch.empty((nnzb,), dtype=torch.float64, device=dev)
     Ft = torch.empty((N, 3), dtype=torch.float64, device=dev)
     wsb = model.workspace()
+    algo = _lib.ALGO_DD if a.algo == "dd" else _lib.ALGO_FP64
     out = _lib.FemAssemblyOut(_lib.LAYOUT_BSR, _lib.LAYOUT_BSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
-                              model.fixed.data_ptr(), model.loads.data_ptr())
+                              model.fixed.data_ptr(), model.loads.data_ptr(), algo)
     st = _stream(dev)
     stream = torch.cuda.current_stream(dev)
     mesh_c, mat_c = ctypes.byref(model.mesh.c), ctypes.byref(model.mat)
@@ -246,7 +248,7 @@ def main():
     def step(ev=None):
         if ev is not None:
             ev[0].record(stream)
-        _lib.check(L.fem_assemble_elements(mesh_c, mat_c, _dptr(wsb), wsb.numel(), st), "elements")
+        _lib.check(L.fem_assemble_elements(mesh_c, mat_c, algo, _dptr(wsb), wsb.numel(), st), "elements")
         if ev is not None:
             ev[1].record(stream)
         _lib.check(L.fem_assemble_gather(mesh_c, ctypes.byref(out), _dptr(wsb), wsb.numel(), st), "gather")

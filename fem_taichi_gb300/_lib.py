@@ -29,6 +29,8 @@ FEM_ERR_BREAKDOWN = -8
 
 LAYOUT_BSR = 0
 LAYOUT_CSR = 1
+ALGO_DD = 0
+ALGO_FP64 = 1
 FEM_F64 = 0
 FEM_F32 = 1
 
@@ -56,7 +58,7 @@ class FemMaterial(ctypes.Structure):
 
 class FemAssemblyOut(ctypes.Structure):
     _fields_ = [("k_layout", c_int), ("m_layout", c_int), ("K", c_void_p), ("M", c_void_p),
-                ("F", c_void_p), ("fixed", c_void_p), ("loads", c_void_p)]
+                ("F", c_void_p), ("fixed", c_void_p), ("loads", c_void_p), ("algo", c_int)]
 
 
 class FemBsr(ctypes.Structure):
@@ -90,8 +92,8 @@ SIGNATURES = {
     "fem_assemble_workspace_bytes": (c_size_t, [c_int64]),
     "fem_assemble": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial),
                              ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t, c_void_p]),
-    "fem_assemble_elements": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_size_t,
-                                      c_void_p]),
+    "fem_assemble_elements": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_int, c_void_p,
+                                      c_size_t, c_void_p]),
     "fem_assemble_gather": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t,
                                     c_void_p]),
     "fem_diag_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p]),
@@ -120,6 +122,8 @@ SIGNATURES = {
     "fem_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_learned_blocks": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_stress_ex": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_void_p]),
     "fem_stress_noalloc": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p]),
     "fem_stress_workspace_bytes": (c_size_t, [c_int64]),

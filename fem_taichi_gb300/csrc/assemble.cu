@@ -392,11 +392,18 @@ int check_assembly_inputs(const fem_mesh* mesh, const fem_material* mat, void* w
 
 }  // namespace
 
-extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, void* workspace,
+namespace fem {
+int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st);
+int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st);
+}  // namespace fem
+
+extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int algo, void* workspace,
                                      size_t workspace_bytes, void* stream) {
     int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
     if (rc) return rc;
+    FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
     if (mesh->n_elem == 0) return FEM_OK;
+    if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream));
     ElemParams ep;
     ep.xyz = mesh->xyz;
     ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
@@ -426,11 +433,13 @@ extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out*
     FEM_REQUIRE(out != nullptr, "out is NULL");
     FEM_REQUIRE(out->k_layout == FEM_LAYOUT_BSR || out->k_layout == FEM_LAYOUT_CSR, "bad k_layout");
     FEM_REQUIRE(out->m_layout == FEM_LAYOUT_BSR || out->m_layout == FEM_LAYOUT_CSR, "bad m_layout");
+    FEM_REQUIRE(out->algo == FEM_ALGO_DD || out->algo == FEM_ALGO_FP64, "bad algo");
     if (workspace_bytes < fem_assemble_workspace_bytes(mesh->n_elem) || (mesh->n_elem && !workspace)) {
         set_error("workspace too small: need %zu bytes", fem_assemble_workspace_bytes(mesh->n_elem));
         return FEM_ERR_WORKSPACE;
     }
     if (mesh->n_node == 0 || (!out->K && !out->M && !out->F)) return FEM_OK;
+    if (out->algo == FEM_ALGO_DD) return launch_gather_dd(mesh, out, workspace, as_stream(stream));
     GatherParams gp;
     gp.n_node = mesh->n_node;
     gp.indptr = mesh->indptr;
@@ -460,7 +469,7 @@ extern "C" int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const
     FEM_REQUIRE(out->k_layout == FEM_LAYOUT_BSR || out->k_layout == FEM_LAYOUT_CSR, "bad k_layout");
     FEM_REQUIRE(out->m_layout == FEM_LAYOUT_BSR || out->m_layout == FEM_LAYOUT_CSR, "bad m_layout");
     if (mesh->n_node == 0) return FEM_OK;
-    rc = fem_assemble_elements(mesh, mat, workspace, workspace_bytes, stream);
+    rc = fem_assemble_elements(mesh, mat, out->algo, workspace, workspace_bytes, stream);
     if (rc) return rc;
     return fem_assemble_gather(mesh, out, workspace, workspace_bytes, stream);
 }

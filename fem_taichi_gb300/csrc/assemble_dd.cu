@@ -1,0 +1,574 @@
+// Hex8 K / M / F assembly, double-float variant (FEM_ALGO_DD, the default).
+//
+// Same two-phase, atomic-free structure and the same per-element record layout as the FP64
+// kernels in assemble.cu, but the element integrals and the gather sums run in double-float
+// arithmetic (fem_dd.cuh) on the FP32 pipes, because FP64 throughput is the binding limit
+// of these kernels on GB300.  Only the inputs are split from FP64 (node coordinates are
+// first made element-local in FP64, so the ~48-bit double-float precision applies to
+// element-size quantities) and only the outputs are formed in FP64 (integer assembly of
+// the double nearest below hi + lo).
+//
+//  k_hex8_element_dd -- 8 threads per element, 16 elements per CTA, as k_hex8_element:
+//     phase A per Gauss point (J, adjugate, det, 1/det, R_a = dN_a/dxi . adj J, R_a/det,
+//     centrifugal density), phase B per node pair (Gram P_ab -> K_ab, M_ab) and per corner
+//     (F_a).  Record: 384 float pairs per element (36 x [K 3x3, M] + 8 x F).
+//  k_gather_dd -- one warp per 4 block rows, lane = (row, element corner): for every
+//     incident element (ascending element index, the fixed order that makes the sums
+//     reproducible), each of the 8 lanes of a row adds one element block into the row's
+//     shared-memory accumulator at the slot of its corner node (binary search in the
+//     row's sorted columns).  All lanes do useful work; a repeated corner of a degenerate
+//     element is added after the first occurrence.  Rows with more than 32 blocks use a
+//     lane-per-slot path.  The penalty and nodal loads are applied when the rows are
+//     written (BSR or the reference CSR order, coalesced).
+#include <climits>
+
+#include "fem_common.cuh"
+#include "fem_dd.cuh"
+
+namespace fem {
+namespace {
+
+constexpr int kEpc = 16;
+constexpr int kElemThreads = kEpc * 8;
+constexpr int kRec = 384;
+constexpr int kPairStride = 10;
+constexpr int kFOff = 36 * kPairStride;
+constexpr int kRPad = 25;
+
+struct DdTables {
+    float2 dnr[8][8][3];
+    float2 nr[8][8];
+    float2 nn[36][8];  // N_a(g) N_b(g) for pair (a <= b), Gauss point g
+};
+
+struct ElemDdParams {
+    const double* xyz;
+    const int4* conn4;
+    int64_t n_elem;
+    float2* rec;
+    float2 DE, D0d, lam, mu, lm;
+    float2 wc[3][3];  // f = wc . x, the centrifugal operator -w x (w x .) of UnitVectorF
+    DdTables tab;
+};
+
+struct ElemDdSmem {
+    float2 dnr[8][8][3];
+    float2 nr[8][8];
+    float2 nn[36][8];
+    float2 xl[kEpc][8][3];
+    float2 x0[kEpc][3];
+    float2 R[kEpc][8][kRPad];
+    float2 Rs[kEpc][8][kRPad];
+    float2 det[kEpc][8];
+    float2 c[kEpc][8][3];
+};
+
+__device__ __forceinline__ dd ld(const float2& v) { return dd{v.x, v.y}; }
+__device__ __forceinline__ float2 st(dd v) { return make_float2(v.hi, v.lo); }
+
+__device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
+    int aa = 0, rem = q;
+    while (rem >= 7 - aa) {
+        rem -= 7 - aa;
+        ++aa;
+    }
+    a = aa;
+    b = aa + 1 + rem;
+}
+
+__global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ElemDdSmem& s = *reinterpret_cast<ElemDdSmem*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int el = tid >> 3;
+    const int t = tid & 7;
+    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.n_elem;
+
+    for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
+    for (int k = tid; k < 64; k += kElemThreads) (&s.nr[0][0])[k] = (&p.tab.nr[0][0])[k];
+    for (int k = tid; k < 36 * 8; k += kElemThreads) (&s.nn[0][0])[k] = (&p.tab.nn[0][0])[k];
+    if (valid) {
+        const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
+        const int64_t node = __ldg(cn + t), node0 = __ldg(cn);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const double x0 = __ldg(p.xyz + 3 * node0 + i);
+            const double x = __ldg(p.xyz + 3 * node + i);
+            s.xl[el][t][i] = st(dd_from_double(x - x0));  // element-local, exact in FP64
+            if (t == 0) s.x0[el][i] = st(dd_from_double(x0));
+        }
+    }
+    __syncthreads();
+
+    // ---- phase A: Gauss point g = t ----------------------------------------------------
+    if (valid) {
+        const int g = t;
+        dd J[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                dd_acc acc = acc_zero();
+#pragma unroll
+                for (int a = 0; a < 8; ++a) acc_fma(acc, ld(s.xl[el][a][i]), ld(s.dnr[g][a][d]));
+                J[i][d] = acc_value(acc);
+            }
+        dd A[3][3];  // adjugate
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+                dd_acc acc = acc_zero();
+                acc_fma(acc, J[i1][j1], J[i2][j2]);
+                acc_fma(acc, dd_neg(J[i2][j1]), J[i1][j2]);
+                A[j][i] = acc_value(acc);
+            }
+        dd_acc da = acc_zero();
+        acc_fma(da, J[0][0], A[0][0]);
+        acc_fma(da, J[1][0], A[0][1]);
+        acc_fma(da, J[2][0], A[0][2]);
+        const dd det = acc_value(da);
+        const dd inv = dd_rcp(det);
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                dd_acc acc = acc_zero();
+                acc_fma(acc, ld(s.dnr[g][a][0]), A[0][i]);
+                acc_fma(acc, ld(s.dnr[g][a][1]), A[1][i]);
+                acc_fma(acc, ld(s.dnr[g][a][2]), A[2][i]);
+                const dd r = acc_value(acc);
+                s.R[el][g][3 * a + i] = st(r);
+                s.Rs[el][g][3 * a + i] = st(dd_mul(r, inv));
+            }
+        s.det[el][g] = st(det);
+        dd X[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            dd_acc acc = acc_zero();
+            acc_add(acc, ld(s.x0[el][i]));
+#pragma unroll
+            for (int a = 0; a < 8; ++a) acc_fma(acc, ld(s.nr[g][a]), ld(s.xl[el][a][i]));
+            X[i] = acc_value(acc);
+        }
+        const dd jd = dd_mul(ld(p.DE), det);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            dd_acc acc = acc_zero();
+#pragma unroll
+            for (int j = 0; j < 3; ++j) acc_fma(acc, ld(p.wc[i][j]), X[j]);
+            s.c[el][g][i] = st(dd_mul(jd, acc_value(acc)));
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+
+    // ---- phase B: node pairs and corner loads -----------------------------------------------
+    float2* rec = p.rec + e * kRec;
+    const dd lam = ld(p.lam), mu = ld(p.mu), D0d = ld(p.D0d), DE = ld(p.DE), lm = ld(p.lm);
+    {
+        const int a = t, pi = pair_index(a, a);
+        dd_acc P00 = acc_zero(), P11 = acc_zero(), P22 = acc_zero(), P01 = acc_zero(), P02 = acc_zero(),
+               P12 = acc_zero(), m = acc_zero();
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const dd r0 = ld(s.R[el][g][3 * a]), r1 = ld(s.R[el][g][3 * a + 1]), r2 = ld(s.R[el][g][3 * a + 2]);
+            const dd q0 = ld(s.Rs[el][g][3 * a]), q1 = ld(s.Rs[el][g][3 * a + 1]), q2 = ld(s.Rs[el][g][3 * a + 2]);
+            acc_fma(P00, q0, r0);
+            acc_fma(P11, q1, r1);
+            acc_fma(P22, q2, r2);
+            acc_fma(P01, q0, r1);
+            acc_fma(P02, q0, r2);
+            acc_fma(P12, q1, r2);
+            acc_fma(m, ld(s.det[el][g]), ld(s.nn[pi][g]));
+        }
+        const dd p00 = acc_value(P00), p11 = acc_value(P11), p22 = acc_value(P22);
+        float2* o = rec + pi * kPairStride;
+        auto diag = [&](dd pp, dd qq, dd rr) {
+            dd_acc acc = acc_zero();
+            acc_fma(acc, D0d, pp);
+            acc_fma(acc, mu, qq);
+            acc_fma(acc, mu, rr);
+            return st(acc_value(acc));
+        };
+        o[0] = diag(p00, p11, p22);
+        o[4] = diag(p11, p00, p22);
+        o[8] = diag(p22, p00, p11);
+        o[1] = o[3] = st(dd_mul(lm, acc_value(P01)));
+        o[2] = o[6] = st(dd_mul(lm, acc_value(P02)));
+        o[5] = o[7] = st(dd_mul(lm, acc_value(P12)));
+        o[9] = st(dd_mul(DE, acc_value(m)));
+    }
+    for (int q = t; q < 28; q += 8) {
+        int a, b;
+        offdiag_pair(q, a, b);
+        const int pi = pair_index(a, b);
+        dd_acc P[3][3], m = acc_zero();
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) P[i][k] = acc_zero();
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            dd qa[3], rb[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                qa[i] = ld(s.Rs[el][g][3 * a + i]);
+                rb[i] = ld(s.R[el][g][3 * b + i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) acc_fma(P[i][k], qa[i], rb[k]);
+            acc_fma(m, ld(s.det[el][g]), ld(s.nn[pi][g]));
+        }
+        dd Pv[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) Pv[i][k] = acc_value(P[i][k]);
+        float2* o = rec + pi * kPairStride;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            dd_acc acc = acc_zero();
+            acc_fma(acc, D0d, Pv[i][i]);
+            acc_fma(acc, mu, Pv[(i + 1) % 3][(i + 1) % 3]);
+            acc_fma(acc, mu, Pv[(i + 2) % 3][(i + 2) % 3]);
+            o[4 * i] = st(acc_value(acc));
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (i == k) continue;
+                dd_acc acc = acc_zero();
+                acc_fma(acc, lam, Pv[i][k]);
+                acc_fma(acc, mu, Pv[k][i]);
+                o[3 * i + k] = st(acc_value(acc));
+            }
+        o[9] = st(dd_mul(DE, acc_value(m)));
+    }
+    {
+        dd_acc f0 = acc_zero(), f1 = acc_zero(), f2 = acc_zero();
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const dd n = ld(s.nr[g][t]);
+            acc_fma(f0, n, ld(s.c[el][g][0]));
+            acc_fma(f1, n, ld(s.c[el][g][1]));
+            acc_fma(f2, n, ld(s.c[el][g][2]));
+        }
+        rec[kFOff + 3 * t + 0] = st(acc_value(f0));
+        rec[kFOff + 3 * t + 1] = st(acc_value(f1));
+        rec[kFOff + 3 * t + 2] = st(acc_value(f2));
+    }
+}
+
+// ---- gather ---------------------------------------------------------------------------------
+
+struct GatherDdParams {
+    int64_t n_node;
+    const int32_t* indptr;
+    const int32_t* indices;
+    const int32_t* ne_ptr;
+    const int32_t* ne_list;
+    const int32_t* conn;
+    const float2* rec;
+    int k_layout, m_layout;
+    double* K;
+    double* M;
+    double* F;
+    const uint8_t* fixed;
+    const double* loads;
+};
+
+
+// element block (a, b) of element e as 10 dd values (K row-major for the a-row, then M)
+__device__ __forceinline__ void load_block(const float2* rec, int64_t e, int a, int b, dd (&v)[kPairStride]) {
+    const int lo = min(a, b), hi = max(a, b);
+    const float4* blk = reinterpret_cast<const float4*>(rec + e * kRec + pair_index(lo, hi) * kPairStride);
+    float2 w[kPairStride];
+#pragma unroll
+    for (int k = 0; k < kPairStride / 2; ++k) {
+        const float4 f = __ldg(blk + k);
+        w[2 * k] = make_float2(f.x, f.y);
+        w[2 * k + 1] = make_float2(f.z, f.w);
+    }
+    if (a <= b) {
+#pragma unroll
+        for (int k = 0; k < kPairStride; ++k) v[k] = ld(w[k]);
+    } else {
+#pragma unroll
+        for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+            for (int qq = 0; qq < 3; ++qq) v[3 * pp + qq] = ld(w[3 * qq + pp]);
+        v[9] = ld(w[9]);
+    }
+}
+
+constexpr int kGWarps = 4;
+constexpr int kRowsPerWarp = 4;
+constexpr int kMaxL = 32;
+
+struct GatherDdSmem {
+    float acc[kGWarps][kRowsPerWarp][kMaxL][kPairStride][2];
+    int cols[kGWarps][kRowsPerWarp][kMaxL];
+};
+
+__device__ __forceinline__ int find_slot(const int* cols, int L, int node) {
+    int lo = 0, hi = L - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cols[mid] < node) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void smem_accumulate(float (*acc)[2], const dd (&v)[kPairStride]) {
+#pragma unroll
+    for (int k = 0; k < kPairStride; ++k) {
+        float s, e;
+        two_sum(acc[k][0], v[k].hi, s, e);
+        acc[k][0] = s;
+        acc[k][1] = __fadd_rn(acc[k][1], __fadd_rn(e, v[k].lo));
+    }
+}
+
+__device__ __forceinline__ double smem_value(const float (*acc)[2], int k) {
+    return dd_to_double(acc_value(dd_acc{acc[k][0], acc[k][1]}));
+}
+
+// Lane-per-slot path for one row of any length (rows with more than kMaxL blocks): the same
+// order of summation as the fast path.
+__device__ void gather_row_long(const GatherDdParams& p, int64_t row, int lane) {
+    const int64_t rs = p.indptr[row];
+    const int L = p.indptr[row + 1] - int(rs);
+    const int ks = p.ne_ptr[row], ke = p.ne_ptr[row + 1];
+    const unsigned fixed_bits = p.fixed ? p.fixed[row] : 0u;
+    for (int base = 0; base < L; base += 32) {
+        const int l = base + lane;
+        const bool active = l < L;
+        const int col = active ? __ldg(p.indices + rs + l) : -1;
+        dd_acc acc[kPairStride];
+#pragma unroll
+        for (int k = 0; k < kPairStride; ++k) acc[k] = acc_zero();
+        for (int k = ks; k < ke; ++k) {
+            const int ent = __ldg(p.ne_list + k);
+            const int64_t e = ent >> 3;
+            const int a = ent & 7;
+            for (int b = 0; b < 8; ++b) {
+                if (__ldg(p.conn + 8 * e + b) != col) continue;
+                dd v[kPairStride];
+                load_block(p.rec, e, a, b, v);
+#pragma unroll
+                for (int q = 0; q < kPairStride; ++q) acc_add(acc[q], v[q]);
+            }
+        }
+        if (!active) continue;
+        const bool diag = col == int(row);
+        for (int q = 0; q < 9; ++q) {
+            double val = dd_to_double(acc_value(acc[q]));
+            if (diag && (q % 4 == 0) && ((fixed_bits >> (q / 4)) & 1u)) val = 1e20;
+            if (p.K) {
+                if (p.k_layout == FEM_LAYOUT_BSR) p.K[9 * (rs + l) + q] = val;
+                else p.K[9 * rs + int64_t(3 * (q / 3)) * L + 3 * l + (q % 3)] = val;
+            }
+        }
+        if (p.M) {
+            const double mv = dd_to_double(acc_value(acc[9]));
+            if (p.m_layout == FEM_LAYOUT_BSR) p.M[rs + l] = mv;
+            else
+                for (int pp = 0; pp < 3; ++pp) p.M[3 * rs + int64_t(pp) * L + l] = mv;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GatherDdSmem& S = *reinterpret_cast<GatherDdSmem*>(smem_raw);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = lane >> 3, b = lane & 7;
+    const int64_t row0 = (int64_t(blockIdx.x) * kGWarps + w) * kRowsPerWarp;
+    if (row0 >= p.n_node) return;
+    const int64_t row = row0 + r;
+    const bool vrow = row < p.n_node;
+    const int64_t rs = vrow ? p.indptr[row] : 0;
+    const int L = vrow ? p.indptr[row + 1] - int(rs) : 0;
+    const int ks = vrow ? p.ne_ptr[row] : 0;
+    const int cnt = vrow ? p.ne_ptr[row + 1] - ks : 0;
+
+    // ---- F for this row (lanes b < 3): incident corners in element order + nodal loads ----
+    if (p.F && vrow && b < 3) {
+        dd_acc f = acc_zero();
+        for (int k = 0; k < cnt; ++k) {
+            const int ent = __ldg(p.ne_list + ks + k);
+            acc_add(f, ld(p.rec[int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b]));
+        }
+        double fv = dd_to_double(acc_value(f));
+        if (p.loads) fv += p.loads[3 * row + b];
+        p.F[3 * row + b] = fv;
+    }
+    if (!p.K && !p.M) return;
+
+    if (__any_sync(0xffffffffu, L > kMaxL)) {
+        for (int rr = 0; rr < kRowsPerWarp; ++rr)
+            if (row0 + rr < p.n_node) gather_row_long(p, row0 + rr, lane);
+        return;
+    }
+
+    // ---- stage columns, clear accumulators ----------------------------------------------------
+    int* cols = S.cols[w][r];
+    for (int l = b; l < kMaxL; l += 8) cols[l] = l < L ? __ldg(p.indices + rs + l) : INT_MAX;
+    float* accw = &S.acc[w][0][0][0][0];
+    for (int k = lane; k < kRowsPerWarp * kMaxL * kPairStride * 2; k += 32) accw[k] = 0.f;
+    __syncwarp();
+
+    int maxcnt = cnt;
+#pragma unroll
+    for (int off = 8; off < 32; off <<= 1) maxcnt = max(maxcnt, __shfl_xor_sync(0xffffffffu, maxcnt, off));
+    for (int k = 0; k < maxcnt; ++k) {
+        const bool active = k < cnt;
+        int64_t e = 0;
+        int a = 0, nb = -1;
+        if (active) {
+            const int ent = __ldg(p.ne_list + ks + k);
+            e = ent >> 3;
+            a = ent & 7;
+            nb = __ldg(p.conn + 8 * e + b);
+        }
+        // repeated corner nodes (degenerate elements) are added after the first occurrence
+        bool dup = false;
+#pragma unroll
+        for (int bp = 0; bp < 7; ++bp) {
+            const int other = __shfl_sync(0xffffffffu, nb, (lane & ~7) | bp);
+            if (bp < b && other == nb) dup = true;
+        }
+        const int slot = active ? find_slot(cols, L, nb) : 0;
+        if (active && !dup) {
+            dd v[kPairStride];
+            load_block(p.rec, e, a, b, v);
+            smem_accumulate(S.acc[w][r][slot], v);
+        }
+        if (__any_sync(0xffffffffu, active && dup)) {
+            for (int bb = 1; bb < 8; ++bb) {
+                __syncwarp();
+                if (active && dup && b == bb) {
+                    dd v[kPairStride];
+                    load_block(p.rec, e, a, b, v);
+                    smem_accumulate(S.acc[w][r][slot], v);
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    // ---- write the four rows (all lanes, coalesced) ---------------------------------------------
+    for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+        const int64_t rw = row0 + rr;
+        if (rw >= p.n_node) break;
+        const int64_t rrs = __shfl_sync(0xffffffffu, rs, rr * 8);
+        const int LL = __shfl_sync(0xffffffffu, L, rr * 8);
+        const unsigned fixed_bits = p.fixed ? p.fixed[rw] : 0u;
+        const int* cc = S.cols[w][rr];
+        const int sd = find_slot(cc, LL, int(rw));
+        const bool has_diag = LL > 0 && cc[sd] == int(rw);
+        float(*acc)[kPairStride][2] = S.acc[w][rr];
+        if (p.K) {
+            for (int o = lane; o < 9 * LL; o += 32) {
+                int s, q9;
+                if (p.k_layout == FEM_LAYOUT_BSR) {
+                    s = o / 9;
+                    q9 = o - 9 * s;
+                } else {
+                    const int pp = o / (3 * LL), rem = o - 3 * LL * pp;
+                    s = rem / 3;
+                    q9 = 3 * pp + (rem - 3 * s);
+                }
+                double val = smem_value(acc[s], q9);
+                if (has_diag && s == sd && (q9 % 4 == 0) && ((fixed_bits >> (q9 / 4)) & 1u)) val = 1e20;
+                p.K[9 * rrs + o] = val;
+            }
+        }
+        if (p.M) {
+            const int nm = p.m_layout == FEM_LAYOUT_BSR ? LL : 3 * LL;
+            for (int o = lane; o < nm; o += 32) {
+                const int s = p.m_layout == FEM_LAYOUT_BSR ? o : o % LL;
+                p.M[(p.m_layout == FEM_LAYOUT_BSR ? rrs : 3 * rrs) + o] = smem_value(acc[s], 9);
+            }
+        }
+    }
+}
+
+void split_host(double x, float2& out) {
+    const float hi = float(x);
+    out = make_float2(hi, float(x - double(hi)));
+}
+
+}  // namespace
+
+int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st) {
+    ElemDdParams ep;
+    ep.xyz = mesh->xyz;
+    ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+    ep.n_elem = mesh->n_elem;
+    ep.rec = static_cast<float2*>(workspace);
+    const double EX = mat->EX, PO = mat->PO;
+    const double D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // FEM_model_bsr.py:435-437
+    const double lam = EX * PO / (1 + PO) / (1 - 2 * PO);         // :439-445
+    const double mu = EX / 2 / (1 + PO);                          // :447-449
+    split_host(mat->DE, ep.DE);
+    split_host(D0d, ep.D0d);
+    split_host(lam, ep.lam);
+    split_host(mu, ep.mu);
+    split_host(lam + mu, ep.lm);
+    const double w0 = mat->omega[0], w1 = mat->omega[1], w2 = mat->omega[2];
+    const double wc[3][3] = {{w1 * w1 + w2 * w2, -w0 * w1, -w0 * w2},   // UnitVectorF, FEM_model_bsr.py:291-300
+                             {-w1 * w0, w0 * w0 + w2 * w2, -w1 * w2},
+                             {-w2 * w0, -w2 * w1, w1 * w1 + w0 * w0}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) split_host(wc[i][j], ep.wc[i][j]);
+    const ShapeTables& T = shape_tables();
+    for (int g = 0; g < 8; ++g)
+        for (int a = 0; a < 8; ++a) {
+            split_host(T.nr[g][a], ep.tab.nr[g][a]);
+            for (int d = 0; d < 3; ++d) split_host(T.dnr[g][a][d], ep.tab.dnr[g][a][d]);
+        }
+    for (int a = 0; a < 8; ++a)
+        for (int b2 = a; b2 < 8; ++b2)
+            for (int g = 0; g < 8; ++g) split_host(T.nr[g][a] * T.nr[g][b2], ep.tab.nn[pair_index(a, b2)][g]);
+    const size_t smem = sizeof(ElemDdSmem);
+    FEM_CUDA(cudaFuncSetAttribute(k_hex8_element_dd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
+    k_hex8_element_dd<<<unsigned(blocks), kElemThreads, smem, st>>>(ep);
+    FEM_LAUNCH_CHECK("k_hex8_element_dd");
+    return FEM_OK;
+}
+
+int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st) {
+    GatherDdParams gp;
+    gp.n_node = mesh->n_node;
+    gp.indptr = mesh->indptr;
+    gp.indices = mesh->indices;
+    gp.ne_ptr = mesh->ne_ptr;
+    gp.ne_list = mesh->ne_list;
+    gp.conn = mesh->conn;
+    gp.rec = static_cast<const float2*>(workspace);
+    gp.k_layout = out->k_layout;
+    gp.m_layout = out->m_layout;
+    gp.K = out->K;
+    gp.M = out->M;
+    gp.F = out->F;
+    gp.fixed = out->fixed;
+    gp.loads = out->loads;
+    const size_t smem = sizeof(GatherDdSmem);
+    FEM_CUDA(cudaFuncSetAttribute(k_gather_dd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int64_t rows_per_cta = int64_t(kGWarps) * kRowsPerWarp;
+    const int64_t blocks = (mesh->n_node + rows_per_cta - 1) / rows_per_cta;
+    k_gather_dd<<<unsigned(blocks), kGWarps * 32, smem, st>>>(gp);
+    FEM_LAUNCH_CHECK("k_gather_dd");
+    return FEM_OK;
+}
+
+}  // namespace fem

@@ -14,6 +14,7 @@
 #include <mutex>
 
 #include "fem_common.cuh"
+#include "fem_dd.cuh"
 
 namespace fem {
 namespace {
@@ -195,8 +196,14 @@ extern "C" size_t fem_stress_workspace_bytes(int64_t n_elem) {
     return n_elem > 0 ? size_t(n_elem) * 48 * sizeof(double) : 0;
 }
 
-extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
-                          const double* extrap, double* out, void* workspace, size_t workspace_bytes, void* stream) {
+namespace fem {
+int launch_stress_dd(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
+                     const double* extrap, double* out, void* workspace, cudaStream_t st);
+}
+
+extern "C" int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
+                             const double* extrap, double* out, void* workspace, size_t workspace_bytes, int algo,
+                             void* stream) {
     FEM_REQUIRE(mesh && mat && extrap, "mesh/mat/extrap is NULL");
     FEM_REQUIRE(mesh->n_node >= 0 && mesh->n_elem >= 0, "negative mesh size");
     FEM_REQUIRE(mesh->n_elem < (int64_t(1) << 28), "n_elem too large");
@@ -208,7 +215,9 @@ extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const d
         set_error("workspace too small: need %zu bytes", fem_stress_workspace_bytes(mesh->n_elem));
         return FEM_ERR_WORKSPACE;
     }
+    FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
     cudaStream_t st = as_stream(stream);
+    if (algo == FEM_ALGO_DD) return launch_stress_dd(mesh, mat, u, co_elem, extrap, out, workspace, st);
     if (mesh->n_elem) {
         StressParams sp;
         sp.xyz = mesh->xyz;
@@ -232,6 +241,11 @@ extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const d
                                                     static_cast<const double*>(workspace), out);
     FEM_LAUNCH_CHECK("k_stress_node");
     return FEM_OK;
+}
+
+extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
+                          const double* extrap, double* out, void* workspace, size_t workspace_bytes, void* stream) {
+    return fem_stress_ex(mesh, mat, u, co_elem, extrap, out, workspace, workspace_bytes, FEM_ALGO_DD, stream);
 }
 
 // ---- allocation-free variant ------------------------------------------------------------------
@@ -283,3 +297,251 @@ extern "C" int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat,
     // reads it, so nothing in the shared scratch has to be cleared between calls.
     return fem_stress(mesh, mat, u, co_elem, extrap, out, scratch, sizeof(g_stress_scratch), stream);
 }
+
+// ---- double-float variant (FEM_ALGO_DD, the default of fem_stress) -----------------------------
+// Same two kernels and record size as above, with the FP64 arithmetic moved to double-float
+// on the FP32 pipes (fem_dd.cuh): node coordinates and displacements are made element-local
+// in FP64 first (the gradient only depends on differences), the corner values are stored as
+// float pairs, and the node kernel sums, averages and diagonalises in double-float (cyclic
+// Jacobi, threshold 2^-46 of the diagonal), forming the FP64 outputs at the end.
+namespace fem {
+namespace {
+
+struct StressDdParams {
+    const double* xyz;
+    const int4* conn4;
+    const double* u;
+    int64_t n_elem;
+    float2* rec;  // [n_elem][8][6] float pairs
+    float2 D0d, lam, mu;
+    float2 dnr[8][8][3];
+    float2 W[8][8];
+};
+
+struct StressDdSmem {
+    float2 dnr[8][8][3];
+    float2 W[8][8];
+    float2 x[kEpc][8][3];
+    float2 u[kEpc][8][3];
+    float2 sv[kEpc][8][kSvPad];
+};
+
+__device__ __forceinline__ dd ldp(const float2& v) { return dd{v.x, v.y}; }
+__device__ __forceinline__ float2 stp(dd v) { return make_float2(v.hi, v.lo); }
+
+__global__ void __launch_bounds__(kThreads) k_stress_element_dd(const StressDdParams p) {
+    __shared__ StressDdSmem s;
+    const int tid = threadIdx.x;
+    const int el = tid >> 3;
+    const int t = tid & 7;
+    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.n_elem;
+    for (int k = tid; k < 8 * 8 * 3; k += kThreads) (&s.dnr[0][0][0])[k] = (&p.dnr[0][0][0])[k];
+    for (int k = tid; k < 64; k += kThreads) (&s.W[0][0])[k] = (&p.W[0][0])[k];
+    if (valid) {
+        const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
+        const int64_t node = __ldg(cn + t), node0 = __ldg(cn);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s.x[el][t][i] = stp(dd_from_double(__ldg(p.xyz + 3 * node + i) - __ldg(p.xyz + 3 * node0 + i)));
+            s.u[el][t][i] = stp(dd_from_double(__ldg(p.u + 3 * node + i) - __ldg(p.u + 3 * node0 + i)));
+        }
+    }
+    __syncthreads();
+    if (valid) {
+        const int g = t;
+        dd J[3][3], G[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                dd_acc aj = acc_zero(), ag = acc_zero();
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    const dd c = ldp(s.dnr[g][a][d]);
+                    acc_fma(aj, ldp(s.x[el][a][i]), c);
+                    acc_fma(ag, ldp(s.u[el][a][i]), c);
+                }
+                J[i][d] = acc_value(aj);
+                G[i][d] = acc_value(ag);
+            }
+        dd A[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+                dd_acc acc = acc_zero();
+                acc_fma(acc, J[i1][j1], J[i2][j2]);
+                acc_fma(acc, dd_neg(J[i2][j1]), J[i1][j2]);
+                A[j][i] = acc_value(acc);
+            }
+        dd_acc da = acc_zero();
+        acc_fma(da, J[0][0], A[0][0]);
+        acc_fma(da, J[1][0], A[0][1]);
+        acc_fma(da, J[2][0], A[0][2]);
+        const dd inv = dd_rcp(acc_value(da));
+        dd H[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                dd_acc acc = acc_zero();
+                acc_fma(acc, G[i][0], A[0][k]);
+                acc_fma(acc, G[i][1], A[1][k]);
+                acc_fma(acc, G[i][2], A[2][k]);
+                H[i][k] = dd_mul(acc_value(acc), inv);
+            }
+        const dd D0d = ldp(p.D0d), lam = ldp(p.lam), mu = ldp(p.mu);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            dd_acc acc = acc_zero();
+            acc_fma(acc, D0d, H[i][i]);
+            acc_fma(acc, lam, H[(i + 1) % 3][(i + 1) % 3]);
+            acc_fma(acc, lam, H[(i + 2) % 3][(i + 2) % 3]);
+            s.sv[el][g][i] = stp(acc_value(acc));
+        }
+        s.sv[el][g][3] = stp(dd_mul(mu, dd_add(H[0][1], H[1][0])));
+        s.sv[el][g][4] = stp(dd_mul(mu, dd_add(H[1][2], H[2][1])));
+        s.sv[el][g][5] = stp(dd_mul(mu, dd_add(H[0][2], H[2][0])));
+    }
+    __syncthreads();
+    if (!valid) return;
+    const int j = t;
+    float2* o = p.rec + (e * 8 + j) * 6;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        dd_acc acc = acc_zero();
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc_fma(acc, ldp(s.W[j][k]), ldp(s.sv[el][k][c]));
+        o[c] = stp(acc_value(acc));
+    }
+}
+
+// Cyclic Jacobi on a symmetric 3x3 in double-float; returns the eigenvalues descending.
+__device__ void sym3_eig_desc_dd(dd (&a)[3][3], dd& p1, dd& p2, dd& p3) {
+    for (int sweep = 0; sweep < 16; ++sweep) {
+        const float off = fabsf(a[0][1].hi) + fabsf(a[0][2].hi) + fabsf(a[1][2].hi);
+        const float dia = fabsf(a[0][0].hi) + fabsf(a[1][1].hi) + fabsf(a[2][2].hi);
+        if (!(off > 0.f) || off <= 1.4210855e-14f * dia) break;  // 2^-46
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int pp = pq == 2 ? 1 : 0;
+            const int qq = pq == 0 ? 1 : 2;
+            const dd apq = a[pp][qq];
+            if (apq.hi == 0.f) continue;
+            const dd theta = dd_div(dd_sub(a[qq][qq], a[pp][pp]), dd_add(apq, apq));
+            dd tt;
+            if (fabsf(theta.hi) > 1e18f) {
+                tt = dd_rcp(dd_add(theta, theta));
+            } else {
+                const dd r = dd_sqrt(dd_add(dd_mul(theta, theta), dd_from_float(1.f)));
+                tt = dd_rcp(dd_add(dd_abs(theta), r));
+                if (theta.hi < 0.f) tt = dd_neg(tt);
+            }
+            const dd c = dd_rcp(dd_sqrt(dd_add(dd_mul(tt, tt), dd_from_float(1.f))));
+            const dd sn = dd_mul(tt, c);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const dd akp = a[k][pp], akq = a[k][qq];
+                a[k][pp] = dd_sub(dd_mul(c, akp), dd_mul(sn, akq));
+                a[k][qq] = dd_add(dd_mul(sn, akp), dd_mul(c, akq));
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const dd apk = a[pp][k], aqk = a[qq][k];
+                a[pp][k] = dd_sub(dd_mul(c, apk), dd_mul(sn, aqk));
+                a[qq][k] = dd_add(dd_mul(sn, apk), dd_mul(c, aqk));
+            }
+        }
+    }
+    dd e0 = a[0][0], e1 = a[1][1], e2 = a[2][2], tmp;
+    if (dd_lt(e0, e1)) tmp = e0, e0 = e1, e1 = tmp;
+    if (dd_lt(e1, e2)) tmp = e1, e1 = e2, e2 = tmp;
+    if (dd_lt(e0, e1)) tmp = e0, e0 = e1, e1 = tmp;
+    p1 = e0;
+    p2 = e1;
+    p3 = e2;
+}
+
+__global__ void __launch_bounds__(256) k_stress_node_dd(int64_t n_node, const int32_t* __restrict__ ne_ptr,
+                                                        const int32_t* __restrict__ ne_list,
+                                                        const int32_t* __restrict__ co_elem,
+                                                        const float2* __restrict__ rec, double* __restrict__ out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n_node) return;
+    dd_acc acc[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = acc_zero();
+    const int ks = ne_ptr[i], ke = ne_ptr[i + 1];
+    for (int k = ks; k < ke; ++k) {
+        const int ent = __ldg(ne_list + k);
+        const float2* r = rec + (int64_t(ent >> 3) * 8 + (ent & 7)) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc_add(acc[c], ldp(__ldg(r + c)));
+    }
+    double* o = out + 10 * i;
+    const int ce = co_elem[i];
+    if (ce == 0) {  // 0 / 0 as the reference's average (POST_process.py:186)
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+        for (int c = 0; c < 10; ++c) o[c] = nan;
+        return;
+    }
+    const dd inv = dd_rcp(dd_from_float(float(ce)));
+    dd v[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = dd_mul(acc_value(acc[c]), inv);
+    // vector order [xx, yy, zz, xy, yz, xz] (POST_process.py:79-86)
+    dd a[3][3] = {{v[0], v[3], v[5]}, {v[3], v[1], v[4]}, {v[5], v[4], v[2]}};
+    dd p1, p2, p3;
+    sym3_eig_desc_dd(a, p1, p2, p3);
+    const dd d12 = dd_sub(p1, p2), d23 = dd_sub(p2, p3);
+    // "VM" as written at POST_process.py:93-94: (p1-p2)^2 + (p2-p3)^2 + (p3-p2)^2
+    const dd vm = dd_sqrt(dd_add(dd_mul(d12, d12), dd_add(dd_mul(d23, d23), dd_mul(d23, d23))));
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o[c] = dd_to_double(v[c]);
+    o[6] = dd_to_double(p1);
+    o[7] = dd_to_double(p2);
+    o[8] = dd_to_double(p3);
+    o[9] = dd_to_double(vm);
+}
+
+void split2(double x, float2& o) {
+    const float hi = float(x);
+    o = make_float2(hi, float(x - double(hi)));
+}
+
+}  // namespace
+
+int launch_stress_dd(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
+                     const double* extrap, double* out, void* workspace, cudaStream_t st) {
+    if (mesh->n_elem) {
+        StressDdParams sp;
+        sp.xyz = mesh->xyz;
+        sp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+        sp.u = u;
+        sp.n_elem = mesh->n_elem;
+        sp.rec = static_cast<float2*>(workspace);
+        const double EX = mat->EX, PO = mat->PO;
+        split2(EX * (1 - PO) / (1 + PO) / (1 - 2 * PO), sp.D0d);  // POST_process.py:292-302
+        split2(EX * PO / (1 + PO) / (1 - 2 * PO), sp.lam);
+        split2(EX / 2 / (1 + PO), sp.mu);                          // :304-306
+        const ShapeTables& T = shape_tables();
+        for (int g = 0; g < 8; ++g)
+            for (int a = 0; a < 8; ++a)
+                for (int d = 0; d < 3; ++d) split2(T.dnr[g][a][d], sp.dnr[g][a][d]);
+        for (int j = 0; j < 8; ++j)
+            for (int k = 0; k < 8; ++k) split2(extrap[8 * j + k], sp.W[j][k]);
+        const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
+        k_stress_element_dd<<<unsigned(blocks), kThreads, 0, st>>>(sp);
+        FEM_LAUNCH_CHECK("k_stress_element_dd");
+    }
+    const int64_t blocks = (mesh->n_node + 255) / 256;
+    k_stress_node_dd<<<unsigned(blocks), 256, 0, st>>>(mesh->n_node, mesh->ne_ptr, mesh->ne_list, co_elem,
+                                                       static_cast<const float2*>(workspace), out);
+    FEM_LAUNCH_CHECK("k_stress_node_dd");
+    return FEM_OK;
+}
+
+}  // namespace fem

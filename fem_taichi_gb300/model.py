@@ -107,7 +107,7 @@ class Model:
     """Drop-in GPU replacement of the reference FE model (linear part)."""
 
     def __init__(self, name, Physics, Materials, Omegas=(0, 0, 100), Largedisp=False, device="cuda",
-                 extra_loads=None):
+                 extra_loads=None, algo="dd"):
         self.name = name
         self.DE, self.EX, self.PO = Materials['DE'], Materials['EX'], Materials['PO']
         self.OM = np.array(Omegas, dtype=np.float64)
@@ -133,6 +133,9 @@ class Model:
         self._csr_index = None
         self._version = 0          # bumped whenever an assembly input changes
         self._cache = None         # (version, K_csr, M_csr, F) device tensors of the last assembly
+        if algo not in ("dd", "fp64"):
+            raise ValueError("algo must be 'dd' or 'fp64'")
+        self.algo = algo
 
     # -- device-level API --------------------------------------------------------------
     def workspace(self) -> torch.Tensor:
@@ -141,12 +144,14 @@ class Model:
             self._ws = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=self.device)
         return self._ws
 
-    def assemble(self, K=True, M=True, F=True, k_layout="bsr", m_layout="bsr", out=None):
+    def assemble(self, K=True, M=True, F=True, k_layout="bsr", m_layout="bsr", out=None, algo=None):
         """Run the assembly kernels; returns (K, M, F) device tensors (None where skipped).
 
         k_layout 'bsr' -> K (nnzb, 3, 3); 'csr' -> K (9*nnzb,) in the reference CSR order.
         m_layout 'bsr' -> M (nnzb,);       'csr' -> M (3*nnzb,) reference CSR order.
+        algo: 'dd' (double-float element integrals and sums, default) or 'fp64'.
         """
+        algo = self.algo if algo is None else algo
         d = self.device
         nnzb = self.mesh.nnzb
         out = out or {}
@@ -165,7 +170,8 @@ class Model:
                            Kt.data_ptr() if Kt is not None else None,
                            Mt.data_ptr() if Mt is not None else None,
                            Ft.data_ptr() if Ft is not None else None,
-                           self.fixed.data_ptr(), self.loads.data_ptr())
+                           self.fixed.data_ptr(), self.loads.data_ptr(),
+                           _lib.ALGO_DD if algo == "dd" else _lib.ALGO_FP64)
         _lib.check(self.lib.fem_assemble(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), ctypes.byref(o),
                                          _dptr(ws), ws.numel(), _stream(d)), "fem_assemble")
         return Kt, Mt, Ft

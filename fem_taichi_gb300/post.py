@@ -48,7 +48,8 @@ def extrapolation_table(gmat_mode: str = "written") -> np.ndarray:
 class Post:
     """Drop-in for POST_process.Post (stress part)."""
 
-    def __init__(self, name, Physics, Materials, Solutions, gmat_mode="written", device="cuda", mesh=None):
+    def __init__(self, name, Physics, Materials, Solutions, gmat_mode="written", device="cuda", mesh=None,
+                 algo="dd"):
         self.name = name
         self.DE, self.EX, self.PO = Materials['DE'], Materials['EX'], Materials['PO']
         self.Physics = Physics
@@ -59,6 +60,9 @@ class Post:
         self.device = self.mesh.device
         self.mat = material(Materials, (0.0, 0.0, 0.0))
         self.W = np.ascontiguousarray(extrapolation_table(gmat_mode))
+        if algo not in ("dd", "fp64"):
+            raise ValueError("algo must be 'dd' or 'fp64'")
+        self.algo = _lib.ALGO_DD if algo == "dd" else _lib.ALGO_FP64
         self.set_solution(Solutions)
         self._ws = None
 
@@ -74,9 +78,9 @@ class Post:
         if out is None:
             out = torch.empty((self.Num_Node, 10), dtype=torch.float64, device=self.device)
         W = self.W.ctypes.data_as(ctypes.c_void_p)
-        _lib.check(self.lib.fem_stress(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), _dptr(self.u),
-                                       _dptr(self.mesh.co_elem), W, _dptr(out), _dptr(self._ws), self._ws.numel(),
-                                       _stream(self.device)), "fem_stress")
+        _lib.check(self.lib.fem_stress_ex(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), _dptr(self.u),
+                                          _dptr(self.mesh.co_elem), W, _dptr(out), _dptr(self._ws),
+                                          self._ws.numel(), self.algo, _stream(self.device)), "fem_stress_ex")
         return out
 
     def Get_Stress(self) -> np.ndarray:

@@ -80,6 +80,10 @@ typedef struct fem_material {
     double omega[3];    /* global angular velocity about an axis through the origin      */
 } fem_material;
 
+#define FEM_ALGO_DD 0   /* element integrals and gather sums in double-float on the FP32 pipes
+                           (inputs split from FP64, outputs formed in FP64); the default */
+#define FEM_ALGO_FP64 1 /* the same two kernels in native FP64 arithmetic                       */
+
 typedef struct fem_assembly_out {
     int k_layout;          /* FEM_LAYOUT_BSR or FEM_LAYOUT_CSR                            */
     int m_layout;          /* FEM_LAYOUT_BSR or FEM_LAYOUT_CSR                            */
@@ -90,9 +94,10 @@ typedef struct fem_assembly_out {
                               entry set to 1e20, FEM_model_bsr.py:248-259), or NULL       */
     const double* loads;   /* [n_node][3] nodal loads added to F after the element terms
                               (LoadF, FEM_model_bsr.py:220-226), or NULL                   */
+    int algo;              /* FEM_ALGO_DD or FEM_ALGO_FP64                                */
 } fem_assembly_out;
 
-/* Assemble K, M and F for one mesh: element integrals (2x2x2 Gauss, FP64) into a
+/* Assemble K, M and F for one mesh: element integrals (2x2x2 Gauss) into a
  * per-element workspace, then a deterministic, atomic-free gather where one warp owns
  * one block row and sums its incident elements in ascending element order. */
 size_t fem_assemble_workspace_bytes(int64_t n_elem);
@@ -101,7 +106,7 @@ int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const fem_assemb
 /* The two phases of fem_assemble, callable separately (same workspace): element records
  * (UnitMatrixK/M + UnitVectorF, FEM_model_bsr.py:262-300), then the gather into K/M/F
  * (InstallMatrixK/M, InstallVectorF scatter, LoadF, ModifyK; FEM_model_csr.py:150-242). */
-int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, void* workspace,
+int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int algo, void* workspace,
                           size_t workspace_bytes, void* stream);
 int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace,
                         size_t workspace_bytes, void* stream);
@@ -119,6 +124,11 @@ size_t fem_stress_workspace_bytes(int64_t n_elem);
 int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
                const int32_t* co_elem, const double* extrap, double* out, void* workspace,
                size_t workspace_bytes, void* stream);
+/* fem_stress with the arithmetic chosen: FEM_ALGO_DD (double-float on the FP32 pipes, what
+ * fem_stress uses) or FEM_ALGO_FP64 (native FP64). */
+int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, const double* u,
+                  const int32_t* co_elem, const double* extrap, double* out, void* workspace,
+                  size_t workspace_bytes, int algo, void* stream);
 
 /* Same as fem_stress, but for callers that cannot allocate device memory (a plug-in whose
  * host program owns every device buffer, or a loop where cudaMalloc/cudaFree are banned

@@ -37,6 +37,15 @@ def assert_K_close(Kg, Ko, rel=REL):
     assert np.all(dev <= rel * rmax[rows]), f"max rel dev {np.max(dev / np.maximum(rmax[rows], 1e-300))}"
 
 
+@pytest.fixture(scope="module")
+def c2_oracle():
+    P = F.config_mesh("c2")
+    bn = P.Nind[P.Bounds[0][0]]
+    bc = np.zeros((bn.size, 3))
+    Kc, Mc, Fc = C.assemble(P.xyz, P.conn, P.SmNode, P.ReNode, STEEL, (0, 0, 100), bn, bc, nthreads=0)
+    return P, Kc, Mc, Fc
+
+
 def assert_vec_close(x, y, rel=REL):
     s = np.abs(y).max()
     assert np.abs(np.asarray(x) - np.asarray(y)).max() <= rel * s
@@ -59,32 +68,39 @@ def case(request):
     return request.param, P, om, OM
 
 
-def test_K_matches_oracle(case):
+ALGOS = ["dd", "fp64"]
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_K_matches_oracle(case, algo):
     name, P, om, OM = case
-    M = F.Model(name, P, STEEL, Omegas=om)
+    M = F.Model(name, P, STEEL, Omegas=om, algo=algo)
     assert_K_close(M.Get_MatrixKL(), OM.Get_MatrixKL())
     assert M.Get_MatrixK is not None
 
 
-def test_M_matches_oracle(case):
+@pytest.mark.parametrize("algo", ALGOS)
+def test_M_matches_oracle(case, algo):
     name, P, om, OM = case
-    M = F.Model(name, P, STEEL, Omegas=om)
+    M = F.Model(name, P, STEEL, Omegas=om, algo=algo)
     Mg, Mo = M.Get_MatrixM(), OM.Get_MatrixM()
     assert np.array_equal(Mg.indptr, Mo.indptr) and np.array_equal(Mg.indices, Mo.indices)
     assert_vec_close(Mg.data, Mo.data)
 
 
-def test_F_matches_oracle(case):
+@pytest.mark.parametrize("algo", ALGOS)
+def test_F_matches_oracle(case, algo):
     name, P, om, OM = case
-    M = F.Model(name, P, STEEL, Omegas=om)
+    M = F.Model(name, P, STEEL, Omegas=om, algo=algo)
     Fg = M.Get_VectorF()
     assert Fg.shape == (3 * P.Num_Node,)
     assert_vec_close(Fg, OM.Get_VectorF())
 
 
-def test_bsr_layout_equals_csr_and_is_deterministic():
+@pytest.mark.parametrize("algo", ALGOS)
+def test_bsr_layout_equals_csr_and_is_deterministic(algo):
     P = mesh2_physics()
-    M = F.Model("2", P, STEEL)
+    M = F.Model("2", P, STEEL, algo=algo)
     K1, M1, F1 = M.assemble(k_layout="bsr", m_layout="bsr")
     K2, M2, F2 = M.assemble(k_layout="bsr", m_layout="bsr")
     torch.cuda.synchronize()
@@ -106,15 +122,28 @@ def test_extra_float_loads_bypass_int_cast():
     assert_vec_close(M.Get_VectorF(), Fo.reshape(-1))
 
 
-def test_full_size_c2_against_c_oracle():
+def test_degenerate_element_with_repeated_corner():
+    """A wedge-like element listing one node twice: every block the reference adds
+    (both corner copies) must be summed, in both arithmetic variants."""
+    xyz = np.random.default_rng(4).random((12, 3)) * 0.2 + np.array(
+        [[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)] + [[2, 0, 0], [2, 1, 0], [2, 0, 1], [2, 1, 1]])
+    e0 = [3, 2, 0, 1, 7, 6, 4, 5]                      # corner order (+,+,-),(-,+,-),... of the unit cube
+    e1 = [9, 3, 1, 8, 11, 7, 5, 11]                     # last corner repeats node 11
+    P = F.Physics(np.arange(1, 13), xyz, np.array([e0, e1]).T, [[np.array([0, 1]), [0, 0, 0]]], [])
+    OM = O.OracleModel(P, STEEL, (0, 0, 100))
+    for algo in ALGOS:
+        M = F.Model("d", P, STEEL, algo=algo)
+        assert_K_close(M.Get_MatrixKL(), OM.Get_MatrixKL())
+        assert_vec_close(M.Get_MatrixM().data, OM.Get_MatrixM().data)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_full_size_c2_against_c_oracle(algo, c2_oracle):
     """200x200x24 (960,000 elements): the whole BSR K, M and F against the threaded C
     restatement; pattern bit-exact, values at the 1e-12 bar."""
-    P = F.config_mesh("c2")
-    M = F.Model("c2", P, STEEL)
+    P, Kc, Mc, Fc = c2_oracle
+    M = F.Model("c2", P, STEEL, algo=algo)
     Kd, Md, Fd = M.assemble(k_layout="bsr", m_layout="bsr")
-    bn = P.Nind[P.Bounds[0][0]]
-    bc = np.zeros((bn.size, 3))
-    Kc, Mc, Fc = C.assemble(P.xyz, P.conn, P.SmNode, P.ReNode, STEEL, (0, 0, 100), bn, bc, nthreads=0)
     Kg = Kd.cpu().numpy()
     pen = Kc >= 1e19
     assert np.array_equal(Kg[pen], Kc[pen])

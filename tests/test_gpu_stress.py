@@ -23,14 +23,15 @@ def assert_stress_close(S, So, rel=REL):
     assert np.all(dev <= rel * sc), f"max rel dev {np.max(dev / np.maximum(sc, 1e-300))}"
 
 
+@pytest.mark.parametrize("algo", ["dd", "fp64"])
 @pytest.mark.parametrize("mode", ["written", "aliased"])
 @pytest.mark.parametrize("name", ["mesh2", "c1", "twisted"])
-def test_stress_matches_oracle(name, mode):
+def test_stress_matches_oracle(name, mode, algo):
     P = {"mesh2": mesh2_physics, "c1": lambda: F.config_mesh("c1"),
          "twisted": lambda: F.hex_block(6, 5, 3, jitter=0.12, twist_deg=40, seed=4)}[name]()
     rng = np.random.default_rng(17)
     u = rng.uniform(-1e-3, 1e-3, size=(P.Num_Node, 3, 1))
-    S = F.Post(name, P, STEEL, u, gmat_mode=mode).Get_Stress()
+    S = F.Post(name, P, STEEL, u, gmat_mode=mode, algo=algo).Get_Stress()
     assert_stress_close(S, O.oracle_stress(P, STEEL, u, gmat_mode=mode))
 
 
@@ -55,6 +56,20 @@ def test_full_size_c2_stress_against_c_oracle():
     P = F.config_mesh("c2")
     rng = np.random.default_rng(2)
     u = rng.uniform(-1e-3, 1e-3, size=(P.Num_Node, 3))
-    S = F.Post("c2", P, STEEL, u).Get_Stress()
     Sc = C.stress(P.xyz, P.conn, P.CoElem, STEEL, u, O.extrapolation_table("written"), nthreads=0)
-    assert_stress_close(S, Sc)
+    for algo in ("dd", "fp64"):
+        S = F.Post("c2", P, STEEL, u, algo=algo).Get_Stress()
+        assert_stress_close(S, Sc)
+
+
+def test_double_eigenvalues_and_constant_fields():
+    """Uniaxial / hydrostatic stress states have repeated principal values, the hard case
+    for eigenvalue accuracy."""
+    P = F.hex_block(4, 3, 3, jitter=0.1, seed=8)
+    n = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+    for Gd in (np.diag([1e-3, 0.0, 0.0]), np.eye(3) * 1e-3, np.outer(n, n) * 1e-3,
+               np.outer(n, n) * 1e-3 + np.eye(3) * 2e-4):
+        u = P.xyz @ Gd.T
+        for algo in ("dd", "fp64"):
+            S = F.Post("p", P, STEEL, u, algo=algo).Get_Stress()
+            assert_stress_close(S, O.oracle_stress(P, STEEL, u))
