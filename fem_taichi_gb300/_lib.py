@@ -49,7 +49,7 @@ class FemError(RuntimeError):
 class FemMesh(ctypes.Structure):
     _fields_ = [("n_node", c_int64), ("n_elem", c_int64), ("nnzb", c_int64),
                 ("xyz", c_void_p), ("conn", c_void_p), ("indptr", c_void_p), ("indices", c_void_p),
-                ("ne_ptr", c_void_p), ("ne_list", c_void_p)]
+                ("ne_ptr", c_void_p), ("ne_list", c_void_p), ("ne_inv", c_void_p), ("slot_map", c_void_p)]
 
 
 class FemMaterial(ctypes.Structure):
@@ -89,6 +89,8 @@ SIGNATURES = {
     "fem_pattern_count": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p]),
     "fem_pattern_fill": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p]),
     "fem_incidence_build": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_gather_map": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_void_p]),
     "fem_assemble_workspace_bytes": (c_size_t, [c_int64]),
     "fem_assemble": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial),
                              ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t, c_void_p]),

@@ -372,7 +372,9 @@ int check_mesh(const fem_mesh* m) {
 using namespace fem;
 
 extern "C" size_t fem_assemble_workspace_bytes(int64_t n_elem) {
-    return n_elem > 0 ? size_t(n_elem) * kRec * sizeof(double) : 0;
+    // FEM_ALGO_FP64: one 3,072-byte record per element; FEM_ALGO_DD: eight 672-byte
+    // row-ordered chunks per element.  The larger of the two serves both.
+    return n_elem > 0 ? size_t(n_elem) * 8 * 672 : 0;
 }
 
 namespace {
@@ -403,6 +405,8 @@ extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* m
     if (rc) return rc;
     FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
     if (mesh->n_elem == 0) return FEM_OK;
+    FEM_REQUIRE(algo != FEM_ALGO_DD || (mesh->ne_inv && mesh->slot_map),
+                "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
     if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream));
     ElemParams ep;
     ep.xyz = mesh->xyz;
@@ -439,7 +443,10 @@ extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out*
         return FEM_ERR_WORKSPACE;
     }
     if (mesh->n_node == 0 || (!out->K && !out->M && !out->F)) return FEM_OK;
-    if (out->algo == FEM_ALGO_DD) return launch_gather_dd(mesh, out, workspace, as_stream(stream));
+    if (out->algo == FEM_ALGO_DD) {
+        FEM_REQUIRE(mesh->n_elem == 0 || mesh->slot_map, "FEM_ALGO_DD needs mesh->slot_map (fem_gather_map)");
+        return launch_gather_dd(mesh, out, workspace, as_stream(stream));
+    }
     GatherParams gp;
     gp.n_node = mesh->n_node;
     gp.indptr = mesh->indptr;

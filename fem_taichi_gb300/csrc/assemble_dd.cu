@@ -30,10 +30,14 @@ namespace {
 
 constexpr int kEpc = 16;
 constexpr int kElemThreads = kEpc * 8;
-constexpr int kRec = 384;
 constexpr int kPairStride = 10;
-constexpr int kFOff = 36 * kPairStride;
 constexpr int kRPad = 25;
+// Row-ordered contribution chunk of one (element e, corner a): the 8 blocks K_e(a, b) with
+// M_e(a, b) (10 float pairs each, b = 0..7), then F_e(a) (3 pairs), padded to 84 pairs
+// (672 bytes).  Chunk k of the workspace belongs to entry k of ne_list, so a block row's
+// contributions are contiguous, in ascending element order.
+constexpr int kChunk = 84;
+constexpr int kChunkF = 80;
 
 struct DdTables {
     float2 dnr[8][8][3];
@@ -44,6 +48,7 @@ struct DdTables {
 struct ElemDdParams {
     const double* xyz;
     const int4* conn4;
+    const int32_t* ne_inv;
     int64_t n_elem;
     float2* rec;
     float2 DE, D0d, lam, mu, lm;
@@ -61,10 +66,18 @@ struct ElemDdSmem {
     float2 Rs[kEpc][8][kRPad];
     float2 det[kEpc][8];
     float2 c[kEpc][8][3];
+    int pos[kEpc][8];
 };
 
 __device__ __forceinline__ dd ld(const float2& v) { return dd{v.x, v.y}; }
 __device__ __forceinline__ float2 st(dd v) { return make_float2(v.hi, v.lo); }
+
+// 10 float pairs (one block) as five 16-byte stores; dst is 16-byte aligned
+__device__ __forceinline__ void store_block(float2* dst, const float2 (&v)[10]) {
+    float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) d[q] = make_float4(v[2 * q].x, v[2 * q].y, v[2 * q + 1].x, v[2 * q + 1].y);
+}
 
 __device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
     int aa = 0, rem = q;
@@ -98,6 +111,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
             s.xl[el][t][i] = st(dd_from_double(x - x0));  // element-local, exact in FP64
             if (t == 0) s.x0[el][i] = st(dd_from_double(x0));
         }
+        s.pos[el][t] = __ldg(p.ne_inv + 8 * e + t);
     }
     __syncthreads();
 
@@ -166,7 +180,8 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
     if (!valid) return;
 
     // ---- phase B: node pairs and corner loads -----------------------------------------------
-    float2* rec = p.rec + e * kRec;
+    // block (a, b) goes to chunk pos[a] at b; its transpose (a != b) to chunk pos[b] at a
+    auto chunk = [&](int a) { return p.rec + int64_t(s.pos[el][a]) * kChunk; };
     const dd lam = ld(p.lam), mu = ld(p.mu), D0d = ld(p.D0d), DE = ld(p.DE), lm = ld(p.lm);
     {
         const int a = t, pi = pair_index(a, a);
@@ -185,7 +200,6 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
             acc_fma(m, ld(s.det[el][g]), ld(s.nn[pi][g]));
         }
         const dd p00 = acc_value(P00), p11 = acc_value(P11), p22 = acc_value(P22);
-        float2* o = rec + pi * kPairStride;
         auto diag = [&](dd pp, dd qq, dd rr) {
             dd_acc acc = acc_zero();
             acc_fma(acc, D0d, pp);
@@ -193,6 +207,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
             acc_fma(acc, mu, rr);
             return st(acc_value(acc));
         };
+        float2 o[kPairStride];
         o[0] = diag(p00, p11, p22);
         o[4] = diag(p11, p00, p22);
         o[8] = diag(p22, p00, p11);
@@ -200,6 +215,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
         o[2] = o[6] = st(dd_mul(lm, acc_value(P02)));
         o[5] = o[7] = st(dd_mul(lm, acc_value(P12)));
         o[9] = st(dd_mul(DE, acc_value(m)));
+        store_block(chunk(a) + a * kPairStride, o);
     }
     for (int q = t; q < 28; q += 8) {
         int a, b;
@@ -229,14 +245,14 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int k = 0; k < 3; ++k) Pv[i][k] = acc_value(P[i][k]);
-        float2* o = rec + pi * kPairStride;
+        float2 kb[kPairStride];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             dd_acc acc = acc_zero();
             acc_fma(acc, D0d, Pv[i][i]);
             acc_fma(acc, mu, Pv[(i + 1) % 3][(i + 1) % 3]);
             acc_fma(acc, mu, Pv[(i + 2) % 3][(i + 2) % 3]);
-            o[4 * i] = st(acc_value(acc));
+            kb[4 * i] = st(acc_value(acc));
         }
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -246,9 +262,17 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
                 dd_acc acc = acc_zero();
                 acc_fma(acc, lam, Pv[i][k]);
                 acc_fma(acc, mu, Pv[k][i]);
-                o[3 * i + k] = st(acc_value(acc));
+                kb[3 * i + k] = st(acc_value(acc));
             }
-        o[9] = st(dd_mul(DE, acc_value(m)));
+        kb[9] = st(dd_mul(DE, acc_value(m)));
+        float2 kt[kPairStride];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) kt[3 * k + i] = kb[3 * i + k];
+        kt[9] = kb[9];
+        store_block(chunk(a) + b * kPairStride, kb);
+        store_block(chunk(b) + a * kPairStride, kt);
     }
     {
         dd_acc f0 = acc_zero(), f1 = acc_zero(), f2 = acc_zero();
@@ -259,9 +283,10 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
             acc_fma(f1, n, ld(s.c[el][g][1]));
             acc_fma(f2, n, ld(s.c[el][g][2]));
         }
-        rec[kFOff + 3 * t + 0] = st(acc_value(f0));
-        rec[kFOff + 3 * t + 1] = st(acc_value(f1));
-        rec[kFOff + 3 * t + 2] = st(acc_value(f2));
+        float4* of = reinterpret_cast<float4*>(chunk(t) + kChunkF);
+        const float2 v0 = st(acc_value(f0)), v1 = st(acc_value(f1)), v2 = st(acc_value(f2));
+        of[0] = make_float4(v0.x, v0.y, v1.x, v1.y);
+        of[1] = make_float4(v2.x, v2.y, 0.f, 0.f);
     }
 }
 
@@ -272,9 +297,8 @@ struct GatherDdParams {
     const int32_t* indptr;
     const int32_t* indices;
     const int32_t* ne_ptr;
-    const int32_t* ne_list;
-    const int32_t* conn;
-    const float2* rec;
+    const uint8_t* slot_map;
+    const float2* rec;  // row-ordered chunks, one per ne_list entry
     int k_layout, m_layout;
     double* K;
     double* M;
@@ -282,30 +306,6 @@ struct GatherDdParams {
     const uint8_t* fixed;
     const double* loads;
 };
-
-
-// element block (a, b) of element e as 10 dd values (K row-major for the a-row, then M)
-__device__ __forceinline__ void load_block(const float2* rec, int64_t e, int a, int b, dd (&v)[kPairStride]) {
-    const int lo = min(a, b), hi = max(a, b);
-    const float4* blk = reinterpret_cast<const float4*>(rec + e * kRec + pair_index(lo, hi) * kPairStride);
-    float2 w[kPairStride];
-#pragma unroll
-    for (int k = 0; k < kPairStride / 2; ++k) {
-        const float4 f = __ldg(blk + k);
-        w[2 * k] = make_float2(f.x, f.y);
-        w[2 * k + 1] = make_float2(f.z, f.w);
-    }
-    if (a <= b) {
-#pragma unroll
-        for (int k = 0; k < kPairStride; ++k) v[k] = ld(w[k]);
-    } else {
-#pragma unroll
-        for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-            for (int qq = 0; qq < 3; ++qq) v[3 * pp + qq] = ld(w[3 * qq + pp]);
-        v[9] = ld(w[9]);
-    }
-}
 
 constexpr int kGWarps = 4;
 constexpr int kRowsPerWarp = 4;
@@ -326,13 +326,24 @@ __device__ __forceinline__ int find_slot(const int* cols, int L, int node) {
     return lo;
 }
 
-__device__ __forceinline__ void smem_accumulate(float (*acc)[2], const dd (&v)[kPairStride]) {
+// block b of chunk k as 10 raw float pairs (16-byte loads)
+__device__ __forceinline__ void load_chunk_block(const float2* rec, int64_t k, int b, float4 (&v)[kPairStride / 2]) {
+    const float4* blk = reinterpret_cast<const float4*>(rec + k * kChunk + b * kPairStride);
 #pragma unroll
-    for (int k = 0; k < kPairStride; ++k) {
-        float s, e;
-        two_sum(acc[k][0], v[k].hi, s, e);
-        acc[k][0] = s;
-        acc[k][1] = __fadd_rn(acc[k][1], __fadd_rn(e, v[k].lo));
+    for (int q = 0; q < kPairStride / 2; ++q) v[q] = __ldg(blk + q);
+}
+
+__device__ __forceinline__ void smem_accumulate(float (*acc)[2], const float4 (&v)[kPairStride / 2]) {
+#pragma unroll
+    for (int q = 0; q < kPairStride / 2; ++q) {
+        const float hv[2] = {v[q].x, v[q].z}, lv[2] = {v[q].y, v[q].w};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float s, e;
+            two_sum(acc[2 * q + h][0], hv[h], s, e);
+            acc[2 * q + h][0] = s;
+            acc[2 * q + h][1] = __fadd_rn(acc[2 * q + h][1], __fadd_rn(e, lv[h]));
+        }
     }
 }
 
@@ -340,8 +351,8 @@ __device__ __forceinline__ double smem_value(const float (*acc)[2], int k) {
     return dd_to_double(acc_value(dd_acc{acc[k][0], acc[k][1]}));
 }
 
-// Lane-per-slot path for one row of any length (rows with more than kMaxL blocks): the same
-// order of summation as the fast path.
+// Lane-per-slot path for a row of any length (rows with more than kMaxL blocks), same order
+// of summation: chunk by chunk, corner by corner.
 __device__ void gather_row_long(const GatherDdParams& p, int64_t row, int lane) {
     const int64_t rs = p.indptr[row];
     const int L = p.indptr[row + 1] - int(rs);
@@ -350,24 +361,19 @@ __device__ void gather_row_long(const GatherDdParams& p, int64_t row, int lane) 
     for (int base = 0; base < L; base += 32) {
         const int l = base + lane;
         const bool active = l < L;
-        const int col = active ? __ldg(p.indices + rs + l) : -1;
         dd_acc acc[kPairStride];
 #pragma unroll
-        for (int k = 0; k < kPairStride; ++k) acc[k] = acc_zero();
+        for (int q = 0; q < kPairStride; ++q) acc[q] = acc_zero();
         for (int k = ks; k < ke; ++k) {
-            const int ent = __ldg(p.ne_list + k);
-            const int64_t e = ent >> 3;
-            const int a = ent & 7;
             for (int b = 0; b < 8; ++b) {
-                if (__ldg(p.conn + 8 * e + b) != col) continue;
-                dd v[kPairStride];
-                load_block(p.rec, e, a, b, v);
+                if (int(__ldg(p.slot_map + 8 * int64_t(k) + b)) != l) continue;
+                const float2* blk = p.rec + int64_t(k) * kChunk + b * kPairStride;
 #pragma unroll
-                for (int q = 0; q < kPairStride; ++q) acc_add(acc[q], v[q]);
+                for (int q = 0; q < kPairStride; ++q) acc_add(acc[q], ld(__ldg(blk + q)));
             }
         }
         if (!active) continue;
-        const bool diag = col == int(row);
+        const bool diag = __ldg(p.indices + rs + l) == int(row);
         for (int q = 0; q < 9; ++q) {
             double val = dd_to_double(acc_value(acc[q]));
             if (diag && (q % 4 == 0) && ((fixed_bits >> (q / 4)) & 1u)) val = 1e20;
@@ -399,13 +405,10 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
     const int ks = vrow ? p.ne_ptr[row] : 0;
     const int cnt = vrow ? p.ne_ptr[row + 1] - ks : 0;
 
-    // ---- F for this row (lanes b < 3): incident corners in element order + nodal loads ----
+    // ---- F for this row (lanes b < 3): corner loads in element order + nodal loads ----
     if (p.F && vrow && b < 3) {
         dd_acc f = acc_zero();
-        for (int k = 0; k < cnt; ++k) {
-            const int ent = __ldg(p.ne_list + ks + k);
-            acc_add(f, ld(p.rec[int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b]));
-        }
+        for (int k = 0; k < cnt; ++k) acc_add(f, ld(__ldg(p.rec + int64_t(ks + k) * kChunk + kChunkF + b)));
         double fv = dd_to_double(acc_value(f));
         if (p.loads) fv += p.loads[3 * row + b];
         p.F[3 * row + b] = fv;
@@ -418,50 +421,48 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
         return;
     }
 
-    // ---- stage columns, clear accumulators ----------------------------------------------------
-    int* cols = S.cols[w][r];
-    for (int l = b; l < kMaxL; l += 8) cols[l] = l < L ? __ldg(p.indices + rs + l) : INT_MAX;
     float* accw = &S.acc[w][0][0][0][0];
     for (int k = lane; k < kRowsPerWarp * kMaxL * kPairStride * 2; k += 32) accw[k] = 0.f;
+    int* cols = S.cols[w][r];
+    for (int l = b; l < kMaxL; l += 8) cols[l] = l < L ? __ldg(p.indices + rs + l) : INT_MAX;
     __syncwarp();
 
     int maxcnt = cnt;
 #pragma unroll
     for (int off = 8; off < 32; off <<= 1) maxcnt = max(maxcnt, __shfl_xor_sync(0xffffffffu, maxcnt, off));
+    // chunk k of row r: lanes (r, 0..7) read its 8 blocks (640 contiguous bytes); the next
+    // chunk's blocks are in flight while the current one is added
+    float4 cur[kPairStride / 2], nxt[kPairStride / 2];
+    int cur_slot = 0, nxt_slot = 0;
+    if (cnt > 0) {
+        load_chunk_block(p.rec, ks, b, cur);
+        cur_slot = __ldg(p.slot_map + 8 * int64_t(ks) + b);
+    }
     for (int k = 0; k < maxcnt; ++k) {
         const bool active = k < cnt;
-        int64_t e = 0;
-        int a = 0, nb = -1;
-        if (active) {
-            const int ent = __ldg(p.ne_list + ks + k);
-            e = ent >> 3;
-            a = ent & 7;
-            nb = __ldg(p.conn + 8 * e + b);
+        if (k + 1 < cnt) {
+            load_chunk_block(p.rec, ks + k + 1, b, nxt);
+            nxt_slot = __ldg(p.slot_map + 8 * int64_t(ks + k + 1) + b);
         }
-        // repeated corner nodes (degenerate elements) are added after the first occurrence
+        // a repeated corner node (degenerate element) maps two corners to one slot:
+        // the later corner is added after the earlier one
         bool dup = false;
 #pragma unroll
         for (int bp = 0; bp < 7; ++bp) {
-            const int other = __shfl_sync(0xffffffffu, nb, (lane & ~7) | bp);
-            if (bp < b && other == nb) dup = true;
+            const int other = __shfl_sync(0xffffffffu, cur_slot, (lane & ~7) | bp);
+            if (bp < b && other == cur_slot) dup = true;
         }
-        const int slot = active ? find_slot(cols, L, nb) : 0;
-        if (active && !dup) {
-            dd v[kPairStride];
-            load_block(p.rec, e, a, b, v);
-            smem_accumulate(S.acc[w][r][slot], v);
-        }
+        if (active && !dup) smem_accumulate(S.acc[w][r][cur_slot], cur);
         if (__any_sync(0xffffffffu, active && dup)) {
             for (int bb = 1; bb < 8; ++bb) {
                 __syncwarp();
-                if (active && dup && b == bb) {
-                    dd v[kPairStride];
-                    load_block(p.rec, e, a, b, v);
-                    smem_accumulate(S.acc[w][r][slot], v);
-                }
+                if (active && dup && b == bb) smem_accumulate(S.acc[w][r][cur_slot], cur);
             }
         }
         __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kPairStride / 2; ++q) cur[q] = nxt[q];
+        cur_slot = nxt_slot;
     }
 
     // ---- write the four rows (all lanes, coalesced) ---------------------------------------------
@@ -512,6 +513,7 @@ int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* 
     ElemDdParams ep;
     ep.xyz = mesh->xyz;
     ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+    ep.ne_inv = mesh->ne_inv;
     ep.n_elem = mesh->n_elem;
     ep.rec = static_cast<float2*>(workspace);
     const double EX = mat->EX, PO = mat->PO;
@@ -552,8 +554,7 @@ int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const vo
     gp.indptr = mesh->indptr;
     gp.indices = mesh->indices;
     gp.ne_ptr = mesh->ne_ptr;
-    gp.ne_list = mesh->ne_list;
-    gp.conn = mesh->conn;
+    gp.slot_map = mesh->slot_map;
     gp.rec = static_cast<const float2*>(workspace);
     gp.k_layout = out->k_layout;
     gp.m_layout = out->m_layout;

@@ -193,3 +193,49 @@ extern "C" int fem_incidence_build(int64_t n_node, int64_t n_elem, const int32_t
     }
     return FEM_OK;
 }
+
+extern "C" int fem_gather_map(int64_t n_node, int64_t n_elem, const int32_t* conn, const int32_t* indptr,
+                              const int32_t* indices, const int32_t* ne_ptr, const int32_t* ne_list, int32_t* ne_inv,
+                              uint8_t* slot_map) {
+    int rc = check_conn(n_node, n_elem, conn);
+    if (rc) return rc;
+    FEM_REQUIRE(indptr && ne_ptr && ne_list && ne_inv && slot_map, "NULL argument");
+    FEM_REQUIRE(n_elem == 0 || indices, "indices is NULL");
+    // ne_inv[e*8+a] = position of (e, a) in the incidence list of node conn[e][a]
+    for (int64_t k = 0; k < 8 * n_elem; ++k) ne_inv[k] = -1;
+    for (int64_t i = 0; i < n_node; ++i)
+        for (int32_t k = ne_ptr[i]; k < ne_ptr[i + 1]; ++k) {
+            const int32_t ent = ne_list[k];
+            FEM_REQUIRE(ent >= 0 && ent < 8 * n_elem && conn[ent] == i, "incidence does not match conn");
+            ne_inv[ent] = k;
+        }
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t e = 0; e < n_elem; ++e) {
+        for (int a = 0; a < 8; ++a) {
+            const int32_t row = conn[8 * e + a];
+            const int32_t* b0 = indices + indptr[row];
+            const int32_t* b1 = indices + indptr[row + 1];
+            const int64_t pos = ne_inv[8 * e + a];
+            if (pos < 0) {
+                bad = 1;
+                continue;
+            }
+            for (int b = 0; b < 8; ++b) {
+                const int32_t col = conn[8 * e + b];
+                const int32_t* it = std::lower_bound(b0, b1, col);
+                if (it == b1 || *it != col || it - b0 > 255) {
+                    bad = 1;
+                    slot_map[8 * pos + b] = 0;
+                    continue;
+                }
+                slot_map[8 * pos + b] = uint8_t(it - b0);
+            }
+        }
+    }
+    if (bad) {
+        set_error("an element node pair is missing from the pattern, or a block row has more than 256 blocks");
+        return FEM_ERR_PATTERN;
+    }
+    return FEM_OK;
+}

@@ -53,6 +53,21 @@ def build_pattern(conn: np.ndarray, n_node: int):
     return indptr, indices
 
 
+def build_gather_map(conn, indptr, indices, ne_ptr, ne_list, n_node: int):
+    """(ne_inv, slot_map) element-to-block map of the gather via the native topology code."""
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    L = _lib.load()
+    E = conn.shape[0]
+    ne_inv = np.empty(8 * E, dtype=np.int32)
+    slot_map = np.empty(64 * E, dtype=np.uint8)
+    _lib.check(L.fem_gather_map(n_node, E, _ptr(conn), _ptr(np.ascontiguousarray(indptr, dtype=np.int32)),
+                                _ptr(np.ascontiguousarray(indices, dtype=np.int32)),
+                                _ptr(np.ascontiguousarray(ne_ptr, dtype=np.int32)),
+                                _ptr(np.ascontiguousarray(ne_list, dtype=np.int32)), _ptr(ne_inv), _ptr(slot_map)),
+               "fem_gather_map")
+    return ne_inv, slot_map
+
+
 def build_incidence(conn: np.ndarray, n_node: int):
     """(ne_ptr, ne_list, co_elem) via the native topology code."""
     conn = np.ascontiguousarray(conn, dtype=np.int32)
@@ -92,6 +107,8 @@ class Physics:
         self.SmNode, self.ReNode = build_pattern(self.conn, self.Num_Node)
         self.CoNode = np.diff(self.SmNode)
         self.ne_ptr, self.ne_list, self.CoElem = build_incidence(self.conn, self.Num_Node)
+        self.ne_inv, self.slot_map = build_gather_map(self.conn, self.SmNode, self.ReNode, self.ne_ptr,
+                                                      self.ne_list, self.Num_Node)
 
     @property
     def xyz(self) -> np.ndarray:

@@ -60,9 +60,11 @@ class DeviceMesh:
         self.ne_ptr = t(P.ne_ptr, torch.int32)
         self.ne_list = t(P.ne_list, torch.int32)
         self.co_elem = t(P.CoElem.astype(np.int32), torch.int32)
+        self.ne_inv = t(P.ne_inv, torch.int32)
+        self.slot_map = t(P.slot_map, torch.uint8)
         self.c = FemMesh(self.n_node, self.n_elem, self.nnzb, self.xyz.data_ptr(), self.conn.data_ptr(),
                          self.indptr.data_ptr(), self.indices.data_ptr(), self.ne_ptr.data_ptr(),
-                         self.ne_list.data_ptr())
+                         self.ne_list.data_ptr(), self.ne_inv.data_ptr(), self.slot_map.data_ptr())
 
     def set_coordinates(self, xyz) -> None:
         """Replace node coordinates in place (host array or device tensor, (N, 3))."""

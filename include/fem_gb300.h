@@ -63,6 +63,13 @@ int fem_pattern_fill(int64_t n_node, int64_t n_elem, const int32_t* conn, const 
  * co_elem[i] = number of distinct elements touching node i (READ_physics.py:60). */
 int fem_incidence_build(int64_t n_node, int64_t n_elem, const int32_t* conn, int32_t* ne_ptr,
                         int32_t* ne_list, int32_t* co_elem);
+/* Element-to-block map of the gather (the precomputed form of the reference's linear slot
+ * search, FEM_model_bsr.py:171-175): ne_inv[e*8+a] = position k of (e, a) in ne_list, and
+ * slot_map[8*k+b] = slot of node conn[e][b] in block row conn[e][a] (0..255).
+ * FEM_ERR_PATTERN if a pair is absent from the pattern or a row has more than 256 blocks. */
+int fem_gather_map(int64_t n_node, int64_t n_elem, const int32_t* conn, const int32_t* indptr,
+                   const int32_t* indices, const int32_t* ne_ptr, const int32_t* ne_list, int32_t* ne_inv,
+                   uint8_t* slot_map);
 
 /* ---- device mesh descriptor ---------------------------------------------------- */
 typedef struct fem_mesh {
@@ -73,6 +80,8 @@ typedef struct fem_mesh {
     const int32_t* indices; /* [nnzb] */
     const int32_t* ne_ptr;  /* [n_node+1] */
     const int32_t* ne_list; /* [8*n_elem] */
+    const int32_t* ne_inv;  /* [8*n_elem] (fem_gather_map), needed by FEM_ALGO_DD assembly */
+    const uint8_t* slot_map; /* [8*n_elem][8] (fem_gather_map), needed by FEM_ALGO_DD assembly */
 } fem_mesh;
 
 typedef struct fem_material {
@@ -97,9 +106,10 @@ typedef struct fem_assembly_out {
     int algo;              /* FEM_ALGO_DD or FEM_ALGO_FP64                                */
 } fem_assembly_out;
 
-/* Assemble K, M and F for one mesh: element integrals (2x2x2 Gauss) into a
- * per-element workspace, then a deterministic, atomic-free gather where one warp owns
- * one block row and sums its incident elements in ascending element order. */
+/* Assemble K, M and F for one mesh: element integrals (2x2x2 Gauss) into a workspace,
+ * then a deterministic, atomic-free gather that sums every block's element contributions
+ * in ascending element order.  FEM_ALGO_DD writes the contributions row-ordered (chunk k =
+ * entry k of ne_list) and gathers them through mesh->slot_map. */
 size_t fem_assemble_workspace_bytes(int64_t n_elem);
 int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
                  void* workspace, size_t workspace_bytes, void* stream);

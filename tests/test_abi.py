@@ -34,7 +34,7 @@ def test_library_loads_and_exports_all_declared_symbols():
 def test_workspace_sizes():
     L = _lib.load()
     assert L.fem_assemble_workspace_bytes(0) == 0
-    assert L.fem_assemble_workspace_bytes(1000) == 1000 * 384 * 8
+    assert L.fem_assemble_workspace_bytes(1000) == 1000 * 8 * 672
     assert L.fem_stress_workspace_bytes(10) == 10 * 48 * 8
 
 

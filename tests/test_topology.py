@@ -76,3 +76,18 @@ def test_out_of_range_connectivity_is_rejected():
     conn[0, 3] = -1
     with pytest.raises(_lib.FemError):
         build_incidence(conn, 4)
+
+
+def test_gather_map_matches_search():
+    """ne_inv inverts ne_list; slot_map[8k+b] is the position of corner b's node in the row of
+    the entry's node (the reference's linear search, FEM_model_bsr.py:171-175)."""
+    P = mesh2_physics()
+    k = np.arange(P.ne_list.size)
+    assert np.array_equal(P.ne_inv[P.ne_list], k)
+    ent = P.ne_list
+    e, a = ent >> 3, ent & 7
+    rows = P.conn[e, a]
+    for b in range(8):
+        cols = P.conn[e, b]
+        s = P.slot_map.reshape(-1, 8)[k, b].astype(np.int64)
+        assert np.array_equal(P.ReNode[P.SmNode[rows] + s], cols)
