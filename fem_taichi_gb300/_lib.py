@@ -29,6 +29,7 @@ FEM_ERR_BREAKDOWN = -8
 
 LAYOUT_BSR = 0
 LAYOUT_CSR = 1
+LAYOUT_RSOA = 2
 ALGO_DD = 0
 ALGO_FP64 = 1
 FEM_F64 = 0
@@ -63,7 +64,7 @@ class FemAssemblyOut(ctypes.Structure):
 
 class FemBsr(ctypes.Structure):
     _fields_ = [("n_brow", c_int64), ("nnzb", c_int64), ("indptr", c_void_p), ("indices", c_void_p),
-                ("vals", c_void_p), ("dtype", c_int)]
+                ("vals", c_void_p), ("dtype", c_int), ("layout", c_int)]
 
 
 class FemPcgOpts(ctypes.Structure):
@@ -104,6 +105,7 @@ SIGNATURES = {
     "fem_spmv_autotune": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, ctypes.POINTER(c_int),
                                   ctypes.POINTER(ctypes.c_float), c_void_p]),
     "fem_convert_f64_to_f32": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
+    "fem_bsr_to_rsoa_f32": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p]),
     "fem_block_jacobi": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_pcg_workspace_bytes": (c_size_t, [c_int64, c_int, c_int]),
     "fem_pcg_solve": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,

@@ -364,7 +364,7 @@ Layout layout(int64_t n, int R, int mixed) {
 
 unsigned vec_grid(int64_t work) {
     const int64_t need = (work + kThreads - 1) / kThreads;
-    return unsigned(std::max<int64_t>(1, std::min<int64_t>(need, std::min<int64_t>(kMaxCtas, int64_t(sm_count()) * 8))));
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>(need, std::min<int64_t>(kMaxCtas, int64_t(sm_count()) * 2))));
 }
 
 template <typename T>
@@ -392,7 +392,9 @@ void launch_spmv_pq(const BsrView<T>& A, const T* p, T* q, double* part, PcgStat
     switch (spmv_variant(variant).lpr) {
         case 32: k_spmv_pq<T, 32><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
         case 16: k_spmv_pq<T, 16><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
-        default: k_spmv_pq<T, 8><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+        case 8: k_spmv_pq<T, 8><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+        case 4: k_spmv_pq<T, 4><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+        default: k_spmv_pq<T, 2><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
     }
 }
 
@@ -464,7 +466,8 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
     const Layout L = layout(n, R, o->mixed);
     PcgState* st = reinterpret_cast<PcgState*>(ws + L.state);
     double* part = reinterpret_cast<double*>(ws + L.part);
-    BsrView<double> K64{n, A64->indptr, A64->indices, static_cast<const double*>(A64->vals)};
+    BsrView<double> K64{n, A64->indptr, A64->indices, static_cast<const double*>(A64->vals),
+                        A64->layout == FEM_LAYOUT_RSOA};
     const int maxit = std::max(1, o->maxit);
     InnerResult ir{0, FEM_OK};
     PcgState h;
@@ -506,7 +509,8 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
         rc = true_residual(U, q, r);
         if (rc) return rc;
     } else {
-        BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals)};
+        BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
+                           A32->layout == FEM_LAYOUT_RSOA};
         double* y = reinterpret_cast<double*>(ws + L.v64[0]);
         double* r64 = reinterpret_cast<double*>(ws + L.v64[1]);
         float* b32 = reinterpret_cast<float*>(ws + L.v32[0]);

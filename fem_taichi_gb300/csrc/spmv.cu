@@ -26,6 +26,22 @@ __global__ void __launch_bounds__(256) k_spmm(const BsrView<T> A, const T* __res
     spmm_rows<T, R>(A, x, y, false);
 }
 
+// BSR [nnzb][9] FP64 -> row-SoA FP32: value q of slot l of row i at 9*rs + q*L + l
+__global__ void __launch_bounds__(256) k_bsr_to_rsoa_f32(int64_t n, const int32_t* __restrict__ indptr,
+                                                         const double* __restrict__ src, float* __restrict__ dst) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = warp0; i < n; i += nw) {
+        const int64_t rs = indptr[i];
+        const int L = indptr[i + 1] - int(rs);
+        for (int o = lane; o < 9 * L; o += 32) {
+            const int q = o / L, l = o - q * L;
+            dst[9 * rs + o] = float(src[9 * (rs + l) + q]);
+        }
+    }
+}
+
 __global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
         dst[i] = float(src[i]);
@@ -86,7 +102,9 @@ int launch_spmv(const BsrView<T>& A, int nrhs, const T* x, T* y, int variant, cu
         switch (v.lpr) {
             case 32: k_spmv<T, 32><<<grid, v.threads, 0, st>>>(A, x, y); break;
             case 16: k_spmv<T, 16><<<grid, v.threads, 0, st>>>(A, x, y); break;
-            default: k_spmv<T, 8><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            case 8: k_spmv<T, 8><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            case 4: k_spmv<T, 4><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            default: k_spmv<T, 2><<<grid, v.threads, 0, st>>>(A, x, y); break;
         }
     } else {
         const int64_t rows_per_cta = 8 * (32 / nrhs);
@@ -108,6 +126,7 @@ int check_bsr(const fem_bsr* A) {
     FEM_REQUIRE(A != nullptr, "A is NULL");
     FEM_REQUIRE(A->n_brow >= 0 && A->nnzb >= 0, "negative size");
     FEM_REQUIRE(A->dtype == FEM_F64 || A->dtype == FEM_F32, "dtype must be FEM_F64 or FEM_F32");
+    FEM_REQUIRE(A->layout == FEM_LAYOUT_BSR || A->layout == FEM_LAYOUT_RSOA, "layout must be BSR or RSOA");
     if (A->n_brow) FEM_REQUIRE(A->indptr != nullptr, "indptr is NULL");
     if (A->nnzb) FEM_REQUIRE(A->indices && A->vals, "indices/vals is NULL");
     return FEM_OK;
@@ -120,10 +139,12 @@ bool valid_nrhs(int r) { return r == 1 || r == 2 || r == 4 || r == 8 || r == 16 
 int bsr_spmv_any(const fem_bsr* A, int nrhs, const void* x, void* y, int variant, cudaStream_t st) {
     if (A->n_brow == 0) return FEM_OK;
     if (A->dtype == FEM_F64) {
-        BsrView<double> v{A->n_brow, A->indptr, A->indices, static_cast<const double*>(A->vals)};
+        BsrView<double> v{A->n_brow, A->indptr, A->indices, static_cast<const double*>(A->vals),
+                          A->layout == FEM_LAYOUT_RSOA};
         return launch_spmv<double>(v, nrhs, static_cast<const double*>(x), static_cast<double*>(y), variant, st);
     }
-    BsrView<float> v{A->n_brow, A->indptr, A->indices, static_cast<const float*>(A->vals)};
+    BsrView<float> v{A->n_brow, A->indptr, A->indices, static_cast<const float*>(A->vals),
+                     A->layout == FEM_LAYOUT_RSOA};
     return launch_spmv<float>(v, nrhs, static_cast<const float*>(x), static_cast<float*>(y), variant, st);
 }
 
@@ -198,5 +219,18 @@ extern "C" int fem_spmv_autotune(const fem_bsr* A, int nrhs, const void* x, void
     if (rc) return rc;
     *best_variant = bid;
     if (best_ms) *best_ms = best;
+    return FEM_OK;
+}
+
+extern "C" int fem_bsr_to_rsoa_f32(const fem_bsr* A, float* dst, void* stream) {
+    int rc = check_bsr(A);
+    if (rc) return rc;
+    FEM_REQUIRE(A->dtype == FEM_F64 && A->layout == FEM_LAYOUT_BSR, "source must be an FP64 BSR matrix");
+    FEM_REQUIRE(A->n_brow == 0 || dst, "dst is NULL");
+    if (A->n_brow == 0) return FEM_OK;
+    const unsigned grid = unsigned(std::min<int64_t>((A->n_brow + 7) / 8, int64_t(sm_count()) * 16));
+    k_bsr_to_rsoa_f32<<<grid, 256, 0, as_stream(stream)>>>(A->n_brow, A->indptr, static_cast<const double*>(A->vals),
+                                                           dst);
+    FEM_LAUNCH_CHECK("k_bsr_to_rsoa_f32");
     return FEM_OK;
 }

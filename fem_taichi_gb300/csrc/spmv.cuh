@@ -19,8 +19,15 @@ struct BsrView {
     int64_t n;              // block rows
     const int32_t* indptr;  // [n+1]
     const int32_t* indices; // [nnzb]
-    const T* vals;          // [nnzb][3][3]
+    const T* vals;          // [nnzb][3][3] (BSR) or, per block row, [9][row length] (row-SoA)
+    int rsoa;               // 1: row-SoA value layout
 };
+
+// address of value q (0..8) of the block in slot l of the row starting at rs with L blocks
+template <typename T>
+__device__ __forceinline__ const T* block_value(const BsrView<T>& A, int64_t rs, int L, int l, int q) {
+    return A.rsoa ? A.vals + 9 * rs + int64_t(q) * L + l : A.vals + 9 * (rs + l) + q;
+}
 
 // Sum over lanes l' with (l' / G) == (l / G) of a warp split into groups of G lanes.
 template <int G, typename V>
@@ -48,13 +55,14 @@ __device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __res
         if (valid) {
             const int64_t rs = __ldg(A.indptr + row);
             const int L = __ldg(A.indptr + row + 1) - int(rs);
+            const int64_t vs = A.rsoa ? int64_t(L) : 1;  // stride between the 9 values of a block
             for (int l = sl; l < L; l += LPR) {
                 const int64_t c = __ldg(A.indices + rs + l);
-                const T* v = A.vals + 9 * (rs + l);
+                const T* v = block_value(A, rs, L, l, 0);
                 const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-                a0 += __ldg(v + 0) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
-                a1 += __ldg(v + 3) * x0 + __ldg(v + 4) * x1 + __ldg(v + 5) * x2;
-                a2 += __ldg(v + 6) * x0 + __ldg(v + 7) * x1 + __ldg(v + 8) * x2;
+                a0 += __ldg(v + 0 * vs) * x0 + __ldg(v + 1 * vs) * x1 + __ldg(v + 2 * vs) * x2;
+                a1 += __ldg(v + 3 * vs) * x0 + __ldg(v + 4 * vs) * x1 + __ldg(v + 5 * vs) * x2;
+                a2 += __ldg(v + 6 * vs) * x0 + __ldg(v + 7 * vs) * x1 + __ldg(v + 8 * vs) * x2;
             }
         }
         a0 = group_sum<LPR>(a0);
@@ -87,14 +95,15 @@ __device__ __forceinline__ double spmm_rows(const BsrView<T>& A, const T* __rest
         const int64_t rs = __ldg(A.indptr + row);
         const int L = __ldg(A.indptr + row + 1) - int(rs);
         T a0 = 0, a1 = 0, a2 = 0;
+        const int64_t vs = A.rsoa ? int64_t(L) : 1;
         for (int l = 0; l < L; ++l) {
             const int64_t c = __ldg(A.indices + rs + l);
-            const T* v = A.vals + 9 * (rs + l);
+            const T* v = block_value(A, rs, L, l, 0);
             const T* xc = x + 3 * c * R + rhs;
             const T x0 = xc[0], x1 = xc[R], x2 = xc[2 * R];
-            a0 += __ldg(v + 0) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
-            a1 += __ldg(v + 3) * x0 + __ldg(v + 4) * x1 + __ldg(v + 5) * x2;
-            a2 += __ldg(v + 6) * x0 + __ldg(v + 7) * x1 + __ldg(v + 8) * x2;
+            a0 += __ldg(v + 0 * vs) * x0 + __ldg(v + 1 * vs) * x1 + __ldg(v + 2 * vs) * x2;
+            a1 += __ldg(v + 3 * vs) * x0 + __ldg(v + 4 * vs) * x1 + __ldg(v + 5 * vs) * x2;
+            a2 += __ldg(v + 6 * vs) * x0 + __ldg(v + 7 * vs) * x1 + __ldg(v + 8 * vs) * x2;
         }
         T* yr = y + 3 * row * R + rhs;
         yr[0] = a0;
@@ -114,10 +123,10 @@ struct SpmvVariant {
     int threads;  // CTA size
     int ctas_per_sm;
 };
-constexpr int kNumSpmvVariants = 6;
+constexpr int kNumSpmvVariants = 8;
 __host__ __device__ inline SpmvVariant spmv_variant(int id) {
-    const SpmvVariant v[kNumSpmvVariants] = {{32, 256, 8}, {16, 256, 8}, {8, 256, 8},
-                                             {32, 512, 4}, {16, 128, 16}, {8, 512, 4}};
+    const SpmvVariant v[kNumSpmvVariants] = {{32, 256, 8}, {16, 256, 8}, {8, 256, 8},  {32, 512, 4},
+                                             {16, 128, 16}, {8, 512, 4},  {4, 256, 8}, {2, 256, 8}};
     return v[(id >= 0 && id < kNumSpmvVariants) ? id : 0];
 }
 

@@ -52,7 +52,7 @@ class DeviceSystem:
         self.n = model.Num_Node
         self.nnzb = model.mesh.nnzb
         self.A64 = FemBsr(self.n, self.nnzb, model.mesh.indptr.data_ptr(), model.mesh.indices.data_ptr(),
-                          self.K64.data_ptr(), FEM_F64)
+                          self.K64.data_ptr(), FEM_F64, _lib.LAYOUT_BSR)
         self._K32 = None
         self._A32 = None
         self._bj = None
@@ -64,12 +64,13 @@ class DeviceSystem:
         return _stream(self.device)
 
     def K32(self):
+        """FP32 copy of K in the row-SoA layout (coalesced SpMV loads)."""
         if self._K32 is None:
-            self._K32 = torch.empty(self.K64.shape, dtype=torch.float32, device=self.device)
-            _lib.check(self.lib.fem_convert_f64_to_f32(_dptr(self.K64), _dptr(self._K32), self.K64.numel(),
-                                                       self.stream), "fem_convert_f64_to_f32")
+            self._K32 = torch.empty(9 * self.nnzb, dtype=torch.float32, device=self.device)
+            _lib.check(self.lib.fem_bsr_to_rsoa_f32(ctypes.byref(self.A64), _dptr(self._K32), self.stream),
+                       "fem_bsr_to_rsoa_f32")
             self._A32 = FemBsr(self.n, self.nnzb, self.model.mesh.indptr.data_ptr(),
-                               self.model.mesh.indices.data_ptr(), self._K32.data_ptr(), FEM_F32)
+                               self.model.mesh.indices.data_ptr(), self._K32.data_ptr(), FEM_F32, _lib.LAYOUT_RSOA)
         return self._K32
 
     def block_jacobi(self) -> torch.Tensor:
@@ -112,6 +113,8 @@ class DeviceSystem:
                 _lib.check(self.lib.fem_spmv_autotune(ctypes.byref(A), 1, _dptr(x), _dptr(y), 5, ctypes.byref(best),
                                                       ctypes.byref(ms), self.stream), "fem_spmv_autotune")
                 self._variant[key] = best.value
+                self.variant_ms = getattr(self, "variant_ms", {})
+                self.variant_ms[key] = ms.value
         return self._variant[key]
 
     def solve(self, F=None, rtol=1e-10, maxit=50000, mixed=True, precond=None, use_graph=True, unroll=16,

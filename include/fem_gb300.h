@@ -158,12 +158,16 @@ int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat, const doub
 #define FEM_F64 0
 #define FEM_F32 1
 
+#define FEM_LAYOUT_RSOA 2 /* values of block row i stored [9][L_i] from 9*indptr[i] (value q of slot l
+                             at 9*indptr[i] + q*L_i + l): lanes of a row read consecutive words */
+
 typedef struct fem_bsr {
     int64_t n_brow, nnzb;   /* block rows (= nodes), 3x3 blocks                         */
     const int32_t* indptr;  /* [n_brow+1]                                               */
     const int32_t* indices; /* [nnzb]                                                   */
-    const void* vals;       /* [nnzb][3][3] double (FEM_F64) or float (FEM_F32)         */
+    const void* vals;       /* 9*nnzb values, double (FEM_F64) or float (FEM_F32)       */
     int dtype;
+    int layout;             /* FEM_LAYOUT_BSR ([nnzb][3][3]) or FEM_LAYOUT_RSOA         */
 } fem_bsr;
 
 /* y = A x (SOLVE_static.py:36, KL * U).  nrhs in {1,2,4,8,16,32}; x, y: [n_brow][3][nrhs]
@@ -175,6 +179,8 @@ int fem_spmv_autotune(const fem_bsr* A, int nrhs, const void* x, void* y, int re
                       float* best_ms, void* stream);
 /* dst[i] = (float)src[i]: the FP32 copy of K / of preconditioner blocks for the mixed solve. */
 int fem_convert_f64_to_f32(const double* src, float* dst, int64_t n, void* stream);
+/* FP32 row-SoA copy (FEM_LAYOUT_RSOA) of an FP64 BSR matrix: the inner-solve operator. */
+int fem_bsr_to_rsoa_f32(const fem_bsr* A, float* dst, void* stream);
 /* Inverses of the 3x3 diagonal blocks (block-Jacobi preconditioner), FP64 and/or FP32
  * outputs [n_brow][9] (either may be NULL); *n_bad (device int) counts rows whose diagonal
  * block is missing or singular (identity used). */

@@ -62,7 +62,7 @@ def test_autotune_returns_valid_variant(sysm):
     S = sysm[2]
     for fp32 in (False, True):
         v = S.variant(fp32, 1)
-        assert 0 <= v < 6
+        assert 0 <= v < 8
 
 
 @pytest.mark.parametrize("mixed", [False, True])
