@@ -13,9 +13,10 @@ path over that mesh: the element-integral kernel and the deterministic gather ke
            Model.Get_MatrixKL(), Get_MatrixM() and Get_VectorF() return scipy/numpy objects
            (device->host copies included).
   roofline: algorithmic bytes of one assembly (24N + 32E + 80 nnzb + 24N + 4 nnzb + 4(N+1))
-           / measured time, against the measured HBM copy bandwidth; the FP64 roofline of
-           the element kernel (analytic FP64 flops / time vs the measured FMA rate) is
-           reported beside it.
+           / measured time, against the measured HBM copy bandwidth.  Beside it, the element
+           kernel's arithmetic rate in FP64-equivalent operations and its ratio to the
+           measured FP64 pipe rate (the double-float kernel exceeds the FP64 pipe; it is
+           bound by FP32 instruction issue).
   cpu_baseline / --impl reference: the C restatement of the reference algorithm (element
            loop, per-element scratch, linear-search slot lookup, atomic scatter, penalty)
            on all host cores.
@@ -42,7 +43,8 @@ sys.path.insert(0, ROOT)
 METRIC = "K+M assembly Melem/s"
 UNIT = "Melem/s"
 
-# FP64 operations per element issued by k_hex8_element (counted from the kernel source):
+# Arithmetic of one element's integrals in FP64 operations, counted from the FP64 kernel
+# k_hex8_element (the double-float kernel evaluates the same operations in FP32 pairs):
 # phase A per Gauss point: J 72 FMA, adjugate 18, det 3, reciprocal ~10, R 72 (24x3),
 # R/det 24, load density ~40; phase B: 28 off-diagonal pairs x (72 + 4 + 21 + 1) +
 # 8 diagonal pairs x (48 + 8 + 14) + F 192.  Flops count an FMA as 2.
@@ -145,6 +147,22 @@ def dist_setup(backend):
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group(backend=backend)
     return ws, rank, local
+
+
+def max_over_ranks(x, device="cpu"):
+    """Largest x over all ranks of the process group (x itself without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world_size, units_per_rank, seconds):
+    """Units processed by all ranks per second (in millions), timed by the slowest rank."""
+    return world_size * units_per_rank / seconds / 1e6
 
 
 def cpu_threads():
@@ -279,12 +297,9 @@ def main():
     total_ms = t0.elapsed_time(t1)
     el_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
     ga_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_step = total_ms / a.steps
-    value = ws * E * a.steps / (total_ms * 1e-3) / 1e6
+    value = whole_job_rate(ws, E * a.steps, total_ms * 1e-3)
 
     # -- roofline ---------------------------------------------------------------------------
     peak, peak_kind = measured_peaks()
@@ -310,9 +325,12 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "fem_assemble = k_hex8_element + k_gather (one assembly)",
                          "algorithmic_bytes": ab,
-                         "fp64": {"kernel": "k_hex8_element", "achieved_tflops": fp64_ach,
-                                  "peak_tflops_measured": fp64_peak.value, "frac": fp64_ach / fp64_peak.value,
-                                  "flops_per_elem": ELEM_FP64_FLOPS}},
+                         "element_arith": {
+                             "kernel": "k_hex8_element_dd" if a.algo == "dd" else "k_hex8_element",
+                             "arith": "double-float pairs on the FP32 pipes" if a.algo == "dd" else "FP64 pipe",
+                             "fp64_equivalent_tflops": fp64_ach, "fp64_ops_per_elem": ELEM_FP64_FLOPS,
+                             "fp64_pipe_peak_tflops_measured": fp64_peak.value,
+                             "x_fp64_pipe_peak": fp64_ach / fp64_peak.value}},
             "kernels": {"k_hex8_element_ms": el_ms, "k_gather_ms": ga_ms,
                         "share_element": el_ms / (el_ms + ga_ms), "share_gather": ga_ms / (el_ms + ga_ms)},
             "gpu_launches": 2 * a.steps, "clocks": clk}
@@ -341,11 +359,8 @@ def main():
             del r
         torch.cuda.synchronize()
         w1 = time.perf_counter() - w0
-        if ws > 1:
-            tt = torch.tensor([w1], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            w1 = float(tt.item())
-        line["e2e"] = {"value": ws * E * ne / w1 / 1e6, "unit": UNIT, "h2d_bytes_per_step": 24 * N,
+        w1 = max_over_ranks(w1, dev)
+        line["e2e"] = {"value": whole_job_rate(ws, E * ne, w1), "unit": UNIT, "h2d_bytes_per_step": 24 * N,
                        "d2h_bytes_per_step": 72 * nnzb + 24 * nnzb + 24 * N, "steps": ne,
                        "ms_per_step": w1 / ne * 1e3,
                        "path": "Model.set_coordinates(pinned) + Get_MatrixKL + Get_MatrixM + Get_VectorF"}
@@ -379,10 +394,13 @@ def main():
         from fem_taichi_gb300 import study
 
         def brief(r):
-            keep = ("label", "wall_s", "iterations", "outer", "relres", "relerr", "meets_1e-8", "status_text")
-            return {"reference": r["reference"], "solves": [{k: x[k] for k in keep} for x in r["solves"]]}
+            keep = ("label", "wall_s", "iterations", "outer", "relres", "relerr", "meets_1e-8", "status_text",
+                    "ms_per_iteration")
+            return {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
 
-        sol = {"c3": brief(study.c3_study(device=dev))}
+        r3 = study.c3_study(device=dev, peak_gbs=peak)
+        sol = {"c3": brief(r3)}
+        sol["c3"]["spmv"] = r3["spmv"]
         r4, net = study.c4_study(device=dev)
         sol["c4"] = brief(r4)
         sol["c4"]["training"] = r4["training"]

@@ -120,14 +120,45 @@ def compare(S: DeviceSystem, Ur, variants, F=None, target=1e-8):
     return rows
 
 
-def c3_study(device="cuda", rtol=1e-10):
+def spmv_bytes(n, nnzb, value_bytes, nrhs=1):
+    """Algorithmic HBM bytes of one BSR product: values, column indices, row pointers, x, y."""
+    return 9 * value_bytes * nnzb + 4 * nnzb + 4 * (n + 1) + 2 * 3 * n * value_bytes * nrhs
+
+
+def spmv_rates(S: DeviceSystem, reps=20, peak_gbs=None):
+    """CUDA-event time of the autotuned FP64 and FP32 (row-SoA) SpMV on this system's K."""
+    out = {}
+    stream = torch.cuda.current_stream(S.device)
+    for fp32, name, vb in ((False, "fp64", 8), (True, "fp32", 4)):
+        x = torch.ones(3 * S.n, dtype=torch.float32 if fp32 else torch.float64, device=S.device)
+        for _ in range(3):
+            S.spmv(x, fp32=fp32)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            S.spmv(x, fp32=fp32)
+        e1.record(stream)
+        torch.cuda.synchronize(S.device)
+        ms = e0.elapsed_time(e1) / reps
+        b = spmv_bytes(S.n, S.nnzb, vb)
+        out[name] = {"variant": S.variant(fp32, 1), "ms": ms, "algorithmic_bytes": b, "gbs": b / (ms * 1e-3) / 1e9}
+        if peak_gbs:
+            out[name]["frac_hbm"] = out[name]["gbs"] / peak_gbs
+    return out
+
+
+def c3_study(device="cuda", rtol=1e-10, peak_gbs=None):
     P = _mesh.config_mesh("c3")
     extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
     S = DeviceSystem(Model("c3", P, STEEL, device=device, extra_loads=extra))
     Ur, ref = reference_solution(S)
     rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
                            ("mixed_bj", dict(rtol=rtol, mixed=True))])
-    return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows}
+    for r in rows:
+        r["ms_per_iteration"] = 1e3 * r["wall_s"] / max(r["iterations"], 1)
+    return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows,
+            "spmv": spmv_rates(S, peak_gbs=peak_gbs)}
 
 
 def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
