@@ -100,6 +100,11 @@ SIGNATURES = {
     "fem_assemble_gather": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t,
                                     c_void_p]),
     "fem_diag_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p]),
+    "fem_assemble_host": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), ctypes.POINTER(FemAssemblyOut),
+                                  c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  c_size_t, c_void_p]),
+    "fem_pipeline_plan": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                  c_void_p]),
     "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_bsr_spmv": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, c_void_p]),
     "fem_spmv_autotune": (c_int, [ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, ctypes.POINTER(c_int),

@@ -21,6 +21,8 @@
 //     reproducible bit for bit.  The penalty (FEM_model_bsr.py:248-259) and nodal loads
 //     (LoadF, :220-226) are applied in the same pass, and the row is written in either
 //     the BSR block order or the reference's scalar-CSR order (FEM_model_csr.py:150-173).
+#include <vector>
+
 #include "fem_common.cuh"
 
 namespace fem {
@@ -395,8 +397,10 @@ int check_assembly_inputs(const fem_mesh* mesh, const fem_material* mat, void* w
 }  // namespace
 
 namespace fem {
-int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st);
-int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st);
+int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st,
+                           int64_t e_begin, int64_t e_end);
+int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st,
+                     int64_t row_begin, int64_t row_end);
 }  // namespace fem
 
 extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int algo, void* workspace,
@@ -407,7 +411,7 @@ extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* m
     if (mesh->n_elem == 0) return FEM_OK;
     FEM_REQUIRE(algo != FEM_ALGO_DD || (mesh->ne_inv && mesh->slot_map),
                 "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
-    if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream));
+    if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream), 0, mesh->n_elem);
     ElemParams ep;
     ep.xyz = mesh->xyz;
     ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
@@ -445,7 +449,7 @@ extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out*
     if (mesh->n_node == 0 || (!out->K && !out->M && !out->F)) return FEM_OK;
     if (out->algo == FEM_ALGO_DD) {
         FEM_REQUIRE(mesh->n_elem == 0 || mesh->slot_map, "FEM_ALGO_DD needs mesh->slot_map (fem_gather_map)");
-        return launch_gather_dd(mesh, out, workspace, as_stream(stream));
+        return launch_gather_dd(mesh, out, workspace, as_stream(stream), 0, mesh->n_node);
     }
     GatherParams gp;
     gp.n_node = mesh->n_node;
@@ -479,6 +483,89 @@ extern "C" int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const
     rc = fem_assemble_elements(mesh, mat, out->algo, workspace, workspace_bytes, stream);
     if (rc) return rc;
     return fem_assemble_gather(mesh, out, workspace, workspace_bytes, stream);
+}
+
+extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                                 const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
+                                 int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+    int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
+    if (rc) return rc;
+    FEM_REQUIRE(out != nullptr, "out is NULL");
+    FEM_REQUIRE(out->k_layout == FEM_LAYOUT_BSR || out->k_layout == FEM_LAYOUT_CSR, "bad k_layout");
+    FEM_REQUIRE(out->m_layout == FEM_LAYOUT_BSR || out->m_layout == FEM_LAYOUT_CSR, "bad m_layout");
+    FEM_REQUIRE(out->algo == FEM_ALGO_DD || out->algo == FEM_ALGO_FP64, "bad algo");
+    FEM_REQUIRE((!K_host || out->K) && (!M_host || out->M) && (!F_host || out->F),
+                "a host output needs the matching device output in out");
+    FEM_REQUIRE(n_parts >= 1 && row_split && elem_split && block_split, "bad plan");
+    FEM_REQUIRE(row_split[0] == 0 && row_split[n_parts] == mesh->n_node && elem_split[0] == 0 &&
+                    elem_split[n_parts] == mesh->n_elem && block_split[0] == 0 && block_split[n_parts] == mesh->nnzb,
+                "plan does not span the mesh (use fem_pipeline_plan)");
+    for (int q = 0; q < n_parts; ++q)
+        FEM_REQUIRE(row_split[q] <= row_split[q + 1] && elem_split[q] <= elem_split[q + 1] &&
+                        block_split[q] <= block_split[q + 1],
+                    "plan is not monotone");
+    if (mesh->n_node == 0) return FEM_OK;
+    FEM_REQUIRE(out->algo != FEM_ALGO_DD || mesh->n_elem == 0 || (mesh->ne_inv && mesh->slot_map),
+                "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
+    cudaStream_t st = as_stream(stream);
+    const bool dd = out->algo == FEM_ALGO_DD;
+    const int parts = dd ? n_parts : 1;  // the FP64 kernels run as one part
+    std::vector<cudaEvent_t> done(parts, nullptr);
+    cudaStream_t cs = nullptr;
+    cudaEvent_t fin = nullptr;
+    auto cleanup = [&] {
+        for (cudaEvent_t e : done)
+            if (e) cudaEventDestroy(e);
+        if (fin) cudaEventDestroy(fin);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    auto fail = [&](cudaError_t e, const char* what) {
+        cleanup();
+        return cuda_status(e, what);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(e, "cudaStreamCreateWithFlags");
+    // all kernels first (a copy into pageable memory may block the host until it ends)
+    for (int q = 0; q < parts; ++q) {
+        if (dd) {
+            rc = launch_hex8_element_dd(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
+            if (!rc) rc = launch_gather_dd(mesh, out, workspace, st, row_split[q], row_split[q + 1]);
+        } else {
+            rc = fem_assemble(mesh, mat, out, workspace, workspace_bytes, stream);
+        }
+        if (rc) {
+            cleanup();
+            return rc;
+        }
+        if ((e = cudaEventCreateWithFlags(&done[q], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventRecord(done[q], st)) != cudaSuccess)
+            return fail(e, "cudaEventRecord");
+    }
+    const int64_t kq = 9, mq = out->m_layout == FEM_LAYOUT_BSR ? 1 : 3;
+    for (int q = 0; q < parts; ++q) {
+        const int64_t r0 = dd ? row_split[q] : 0, r1 = dd ? row_split[q + 1] : mesh->n_node;
+        const int64_t b0 = dd ? block_split[q] : 0, b1 = dd ? block_split[q + 1] : mesh->nnzb;
+        if ((e = cudaStreamWaitEvent(cs, done[q], 0)) != cudaSuccess) return fail(e, "cudaStreamWaitEvent");
+        if (K_host && b1 > b0 &&
+            (e = cudaMemcpyAsync(K_host + kq * b0, out->K + kq * b0, sizeof(double) * kq * (b1 - b0),
+                                 cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
+            return fail(e, "K device->host copy");
+        if (M_host && b1 > b0 &&
+            (e = cudaMemcpyAsync(M_host + mq * b0, out->M + mq * b0, sizeof(double) * mq * (b1 - b0),
+                                 cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
+            return fail(e, "M device->host copy");
+        if (F_host && r1 > r0 &&
+            (e = cudaMemcpyAsync(F_host + 3 * r0, out->F + 3 * r0, sizeof(double) * 3 * (r1 - r0),
+                                 cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
+            return fail(e, "F device->host copy");
+    }
+    // the caller's stream is ordered after the last copy
+    if ((e = cudaEventCreateWithFlags(&fin, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventRecord(fin, cs)) != cudaSuccess || (e = cudaStreamWaitEvent(st, fin, 0)) != cudaSuccess)
+        return fail(e, "copy completion event");
+    cleanup();
+    return FEM_OK;
 }
 
 extern "C" int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* rowM, int32_t* colM,

@@ -8,18 +8,23 @@
 // element-size quantities) and only the outputs are formed in FP64 (integer assembly of
 // the double nearest below hi + lo).
 //
-//  k_hex8_element_dd -- 8 threads per element, 16 elements per CTA, as k_hex8_element:
+//  k_hex8_element_dd -- 8 threads per element, 16 elements per CTA, 4 CTAs per SM:
 //     phase A per Gauss point (J, adjugate, det, 1/det, R_a = dN_a/dxi . adj J, R_a/det,
 //     centrifugal density), phase B per node pair (Gram P_ab -> K_ab, M_ab) and per corner
-//     (F_a).  Record: 384 float pairs per element (36 x [K 3x3, M] + 8 x F).
+//     (F_a).  Only R and R/det live in shared memory (55.5 KB per CTA); corner coordinates,
+//     det and the load densities move between the 8 threads of an element by warp
+//     shuffles.  Output: one 672-byte chunk per (element, corner a) -- the 8 blocks
+//     K_e(a, b) with M_e(a, b) and F_e(a) -- stored at the position of (e, a) in the
+//     node-to-element incidence list, so each block row's contributions are contiguous
+//     and in ascending element order.
 //  k_gather_dd -- one warp per 4 block rows, lane = (row, element corner): for every
 //     incident element (ascending element index, the fixed order that makes the sums
 //     reproducible), each of the 8 lanes of a row adds one element block into the row's
-//     shared-memory accumulator at the slot of its corner node (binary search in the
-//     row's sorted columns).  All lanes do useful work; a repeated corner of a degenerate
-//     element is added after the first occurrence.  Rows with more than 32 blocks use a
-//     lane-per-slot path.  The penalty and nodal loads are applied when the rows are
-//     written (BSR or the reference CSR order, coalesced).
+//     shared-memory accumulator at the slot given by the precomputed element-to-block map
+//     (slot_map).  All lanes do useful work; a repeated corner of a degenerate element is
+//     added after the first occurrence.  Rows with more than 32 blocks use a lane-per-slot
+//     path.  The penalty and nodal loads are applied when the rows are written (BSR or the
+//     reference CSR order, coalesced).
 #include <climits>
 
 #include "fem_common.cuh"
@@ -49,24 +54,11 @@ struct ElemDdParams {
     const double* xyz;
     const int4* conn4;
     const int32_t* ne_inv;
-    int64_t n_elem;
+    int64_t e_begin, e_end;  // elements [e_begin, e_end) of this launch
     float2* rec;
     float2 DE, D0d, lam, mu, lm;
     float2 wc[3][3];  // f = wc . x, the centrifugal operator -w x (w x .) of UnitVectorF
     DdTables tab;
-};
-
-struct ElemDdSmem {
-    float2 dnr[8][8][3];
-    float2 nr[8][8];
-    float2 nn[36][8];
-    float2 xl[kEpc][8][3];
-    float2 x0[kEpc][3];
-    float2 R[kEpc][8][kRPad];
-    float2 Rs[kEpc][8][kRPad];
-    float2 det[kEpc][8];
-    float2 c[kEpc][8][3];
-    int pos[kEpc][8];
 };
 
 __device__ __forceinline__ dd ld(const float2& v) { return dd{v.x, v.y}; }
@@ -89,18 +81,35 @@ __device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
     b = aa + 1 + rem;
 }
 
-__global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdParams p) {
+struct ElemDdSmem {
+    float2 dnr[8][8][3];
+    float2 nr[8][8];
+    float2 nn[36][8];
+    float2 R[kEpc][8][kRPad];
+    float2 Rs[kEpc][8][kRPad];
+};
+
+__device__ __forceinline__ dd shfl_dd(dd v, int src) {
+    return dd{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+__global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemDdParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ElemDdSmem& s = *reinterpret_cast<ElemDdSmem*>(smem_raw);
     const int tid = threadIdx.x;
     const int el = tid >> 3;
     const int t = tid & 7;
-    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
-    const bool valid = e < p.n_elem;
+    const int base = (tid & 31) & ~7;  // lane of thread 0 of this element
+    const int64_t e = p.e_begin + int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.e_end;
 
     for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
     for (int k = tid; k < 64; k += kElemThreads) (&s.nr[0][0])[k] = (&p.tab.nr[0][0])[k];
     for (int k = tid; k < 36 * 8; k += kElemThreads) (&s.nn[0][0])[k] = (&p.tab.nn[0][0])[k];
+    dd xl[3], x0d[3];  // this thread's corner (element-local) and corner 0 (global)
+    int pos = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) xl[i] = x0d[i] = dd{0.f, 0.f};
     if (valid) {
         const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
         const int64_t node = __ldg(cn + t), node0 = __ldg(cn);
@@ -108,96 +117,115 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
         for (int i = 0; i < 3; ++i) {
             const double x0 = __ldg(p.xyz + 3 * node0 + i);
             const double x = __ldg(p.xyz + 3 * node + i);
-            s.xl[el][t][i] = st(dd_from_double(x - x0));  // element-local, exact in FP64
-            if (t == 0) s.x0[el][i] = st(dd_from_double(x0));
+            xl[i] = dd_from_double(x - x0);  // element-local, exact in FP64
+            x0d[i] = dd_from_double(x0);
         }
-        s.pos[el][t] = __ldg(p.ne_inv + 8 * e + t);
+        pos = __ldg(p.ne_inv + 8 * e + t);
     }
     __syncthreads();
 
-    // ---- phase A: Gauss point g = t ----------------------------------------------------
-    if (valid) {
-        const int g = t;
-        dd J[3][3];
+    // ---- phase A: Gauss point g = t (all lanes run it; lanes of absent elements see zeros) ----
+    const int g = t;
+    dd J[3][3];
+    {
+        dd_acc jacc[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                dd_acc acc = acc_zero();
-#pragma unroll
-                for (int a = 0; a < 8; ++a) acc_fma(acc, ld(s.xl[el][a][i]), ld(s.dnr[g][a][d]));
-                J[i][d] = acc_value(acc);
-            }
-        dd A[3][3];  // adjugate
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-                dd_acc acc = acc_zero();
-                acc_fma(acc, J[i1][j1], J[i2][j2]);
-                acc_fma(acc, dd_neg(J[i2][j1]), J[i1][j2]);
-                A[j][i] = acc_value(acc);
-            }
-        dd_acc da = acc_zero();
-        acc_fma(da, J[0][0], A[0][0]);
-        acc_fma(da, J[1][0], A[0][1]);
-        acc_fma(da, J[2][0], A[0][2]);
-        const dd det = acc_value(da);
-        const dd inv = dd_rcp(det);
-#pragma unroll
-        for (int a = 0; a < 8; ++a)
+            for (int d = 0; d < 3; ++d) jacc[i][d] = acc_zero();
+#pragma unroll 1
+        for (int a = 0; a < 8; ++a) {
+            dd xa[3], da[3];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                dd_acc acc = acc_zero();
-                acc_fma(acc, ld(s.dnr[g][a][0]), A[0][i]);
-                acc_fma(acc, ld(s.dnr[g][a][1]), A[1][i]);
-                acc_fma(acc, ld(s.dnr[g][a][2]), A[2][i]);
-                const dd r = acc_value(acc);
-                s.R[el][g][3 * a + i] = st(r);
-                s.Rs[el][g][3 * a + i] = st(dd_mul(r, inv));
+                xa[i] = shfl_dd(xl[i], base + a);
+                da[i] = ld(s.dnr[g][a][i]);
             }
-        s.det[el][g] = st(det);
-        dd X[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) acc_fma(jacc[i][d], xa[i], da[d]);
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) J[i][d] = acc_value(jacc[i][d]);
+    }
+    dd A[3][3];  // adjugate
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+            dd_acc acc = acc_zero();
+            acc_fma(acc, J[i1][j1], J[i2][j2]);
+            acc_fma(acc, dd_neg(J[i2][j1]), J[i1][j2]);
+            A[j][i] = acc_value(acc);
+        }
+    dd_acc da = acc_zero();
+    acc_fma(da, J[0][0], A[0][0]);
+    acc_fma(da, J[1][0], A[0][1]);
+    acc_fma(da, J[2][0], A[0][2]);
+    const dd det = acc_value(da);
+    const dd inv = dd_rcp(det);
+#pragma unroll 1
+    for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             dd_acc acc = acc_zero();
-            acc_add(acc, ld(s.x0[el][i]));
-#pragma unroll
-            for (int a = 0; a < 8; ++a) acc_fma(acc, ld(s.nr[g][a]), ld(s.xl[el][a][i]));
-            X[i] = acc_value(acc);
+            acc_fma(acc, ld(s.dnr[g][a][0]), A[0][i]);
+            acc_fma(acc, ld(s.dnr[g][a][1]), A[1][i]);
+            acc_fma(acc, ld(s.dnr[g][a][2]), A[2][i]);
+            const dd r = acc_value(acc);
+            s.R[el][g][3 * a + i] = st(r);
+            s.Rs[el][g][3 * a + i] = st(dd_mul(r, inv));
         }
+    dd cg[3];  // DE det f(x_g): centrifugal load density at this Gauss point
+    {
+        dd_acc xacc[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            xacc[i] = acc_zero();
+            acc_add(xacc[i], x0d[i]);
+        }
+#pragma unroll 1
+        for (int a = 0; a < 8; ++a) {
+            const dd n = ld(s.nr[g][a]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) acc_fma(xacc[i], n, shfl_dd(xl[i], base + a));
+        }
+        dd X[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) X[i] = acc_value(xacc[i]);
         const dd jd = dd_mul(ld(p.DE), det);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             dd_acc acc = acc_zero();
 #pragma unroll
             for (int j = 0; j < 3; ++j) acc_fma(acc, ld(p.wc[i][j]), X[j]);
-            s.c[el][g][i] = st(dd_mul(jd, acc_value(acc)));
+            cg[i] = dd_mul(jd, acc_value(acc));
         }
     }
     __syncthreads();
-    if (!valid) return;
 
     // ---- phase B: node pairs and corner loads -----------------------------------------------
     // block (a, b) goes to chunk pos[a] at b; its transpose (a != b) to chunk pos[b] at a
-    auto chunk = [&](int a) { return p.rec + int64_t(s.pos[el][a]) * kChunk; };
     const dd lam = ld(p.lam), mu = ld(p.mu), D0d = ld(p.D0d), DE = ld(p.DE), lm = ld(p.lm);
     {
         const int a = t, pi = pair_index(a, a);
         dd_acc P00 = acc_zero(), P11 = acc_zero(), P22 = acc_zero(), P01 = acc_zero(), P02 = acc_zero(),
                P12 = acc_zero(), m = acc_zero();
-#pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            const dd r0 = ld(s.R[el][g][3 * a]), r1 = ld(s.R[el][g][3 * a + 1]), r2 = ld(s.R[el][g][3 * a + 2]);
-            const dd q0 = ld(s.Rs[el][g][3 * a]), q1 = ld(s.Rs[el][g][3 * a + 1]), q2 = ld(s.Rs[el][g][3 * a + 2]);
+#pragma unroll 1
+        for (int gg = 0; gg < 8; ++gg) {
+            const dd r0 = ld(s.R[el][gg][3 * a]), r1 = ld(s.R[el][gg][3 * a + 1]), r2 = ld(s.R[el][gg][3 * a + 2]);
+            const dd q0 = ld(s.Rs[el][gg][3 * a]), q1 = ld(s.Rs[el][gg][3 * a + 1]), q2 = ld(s.Rs[el][gg][3 * a + 2]);
             acc_fma(P00, q0, r0);
             acc_fma(P11, q1, r1);
             acc_fma(P22, q2, r2);
             acc_fma(P01, q0, r1);
             acc_fma(P02, q0, r2);
             acc_fma(P12, q1, r2);
-            acc_fma(m, ld(s.det[el][g]), ld(s.nn[pi][g]));
+            acc_fma(m, shfl_dd(det, base + gg), ld(s.nn[pi][gg]));
         }
         const dd p00 = acc_value(P00), p11 = acc_value(P11), p22 = acc_value(P22);
         auto diag = [&](dd pp, dd qq, dd rr) {
@@ -215,31 +243,38 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
         o[2] = o[6] = st(dd_mul(lm, acc_value(P02)));
         o[5] = o[7] = st(dd_mul(lm, acc_value(P12)));
         o[9] = st(dd_mul(DE, acc_value(m)));
-        store_block(chunk(a) + a * kPairStride, o);
+        if (valid) store_block(p.rec + int64_t(pos) * kChunk + a * kPairStride, o);
     }
-    for (int q = t; q < 28; q += 8) {
+    // 28 off-diagonal pairs, pair t + 8 it; every lane runs 4 rounds (the shuffles need the
+    // whole warp), lanes without a fourth pair compute a dummy one and store nothing
+#pragma unroll 1
+    for (int it = 0; it < 4; ++it) {
+        const int q = t + 8 * it;
+        const bool act = q < 28;
         int a, b;
-        offdiag_pair(q, a, b);
+        offdiag_pair(act ? q : 27, a, b);
         const int pi = pair_index(a, b);
         dd_acc P[3][3], m = acc_zero();
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int k = 0; k < 3; ++k) P[i][k] = acc_zero();
-#pragma unroll
-        for (int g = 0; g < 8; ++g) {
+#pragma unroll 1
+        for (int gg = 0; gg < 8; ++gg) {
             dd qa[3], rb[3];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                qa[i] = ld(s.Rs[el][g][3 * a + i]);
-                rb[i] = ld(s.R[el][g][3 * b + i]);
+                qa[i] = ld(s.Rs[el][gg][3 * a + i]);
+                rb[i] = ld(s.R[el][gg][3 * b + i]);
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) acc_fma(P[i][k], qa[i], rb[k]);
-            acc_fma(m, ld(s.det[el][g]), ld(s.nn[pi][g]));
+            acc_fma(m, shfl_dd(det, base + gg), ld(s.nn[pi][gg]));
         }
+        const int pos_a = __shfl_sync(0xffffffffu, pos, base + a);
+        const int pos_b = __shfl_sync(0xffffffffu, pos, base + b);
         dd Pv[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -271,29 +306,33 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element_dd(const ElemDdPa
 #pragma unroll
             for (int k = 0; k < 3; ++k) kt[3 * k + i] = kb[3 * i + k];
         kt[9] = kb[9];
-        store_block(chunk(a) + b * kPairStride, kb);
-        store_block(chunk(b) + a * kPairStride, kt);
+        if (valid && act) {
+            store_block(p.rec + int64_t(pos_a) * kChunk + b * kPairStride, kb);
+            store_block(p.rec + int64_t(pos_b) * kChunk + a * kPairStride, kt);
+        }
     }
     {
         dd_acc f0 = acc_zero(), f1 = acc_zero(), f2 = acc_zero();
-#pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            const dd n = ld(s.nr[g][t]);
-            acc_fma(f0, n, ld(s.c[el][g][0]));
-            acc_fma(f1, n, ld(s.c[el][g][1]));
-            acc_fma(f2, n, ld(s.c[el][g][2]));
+#pragma unroll 1
+        for (int gg = 0; gg < 8; ++gg) {
+            const dd n = ld(s.nr[gg][t]);
+            acc_fma(f0, n, shfl_dd(cg[0], base + gg));
+            acc_fma(f1, n, shfl_dd(cg[1], base + gg));
+            acc_fma(f2, n, shfl_dd(cg[2], base + gg));
         }
-        float4* of = reinterpret_cast<float4*>(chunk(t) + kChunkF);
-        const float2 v0 = st(acc_value(f0)), v1 = st(acc_value(f1)), v2 = st(acc_value(f2));
-        of[0] = make_float4(v0.x, v0.y, v1.x, v1.y);
-        of[1] = make_float4(v2.x, v2.y, 0.f, 0.f);
+        if (valid) {
+            float4* of = reinterpret_cast<float4*>(p.rec + int64_t(pos) * kChunk + kChunkF);
+            const float2 v0 = st(acc_value(f0)), v1 = st(acc_value(f1)), v2 = st(acc_value(f2));
+            of[0] = make_float4(v0.x, v0.y, v1.x, v1.y);
+            of[1] = make_float4(v2.x, v2.y, 0.f, 0.f);
+        }
     }
 }
 
 // ---- gather ---------------------------------------------------------------------------------
 
 struct GatherDdParams {
-    int64_t n_node;
+    int64_t row_begin, row_end;  // block rows [row_begin, row_end) of this launch
     const int32_t* indptr;
     const int32_t* indices;
     const int32_t* ne_ptr;
@@ -396,10 +435,10 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
     GatherDdSmem& S = *reinterpret_cast<GatherDdSmem*>(smem_raw);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = lane >> 3, b = lane & 7;
-    const int64_t row0 = (int64_t(blockIdx.x) * kGWarps + w) * kRowsPerWarp;
-    if (row0 >= p.n_node) return;
+    const int64_t row0 = p.row_begin + (int64_t(blockIdx.x) * kGWarps + w) * kRowsPerWarp;
+    if (row0 >= p.row_end) return;
     const int64_t row = row0 + r;
-    const bool vrow = row < p.n_node;
+    const bool vrow = row < p.row_end;
     const int64_t rs = vrow ? p.indptr[row] : 0;
     const int L = vrow ? p.indptr[row + 1] - int(rs) : 0;
     const int ks = vrow ? p.ne_ptr[row] : 0;
@@ -417,7 +456,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
 
     if (__any_sync(0xffffffffu, L > kMaxL)) {
         for (int rr = 0; rr < kRowsPerWarp; ++rr)
-            if (row0 + rr < p.n_node) gather_row_long(p, row0 + rr, lane);
+            if (row0 + rr < p.row_end) gather_row_long(p, row0 + rr, lane);
         return;
     }
 
@@ -468,7 +507,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
     // ---- write the four rows (all lanes, coalesced) ---------------------------------------------
     for (int rr = 0; rr < kRowsPerWarp; ++rr) {
         const int64_t rw = row0 + rr;
-        if (rw >= p.n_node) break;
+        if (rw >= p.row_end) break;
         const int64_t rrs = __shfl_sync(0xffffffffu, rs, rr * 8);
         const int LL = __shfl_sync(0xffffffffu, L, rr * 8);
         const unsigned fixed_bits = p.fixed ? p.fixed[rw] : 0u;
@@ -477,26 +516,34 @@ __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams
         const bool has_diag = LL > 0 && cc[sd] == int(rw);
         float(*acc)[kPairStride][2] = S.acc[w][rr];
         if (p.K) {
-            for (int o = lane; o < 9 * LL; o += 32) {
-                int s, q9;
-                if (p.k_layout == FEM_LAYOUT_BSR) {
-                    s = o / 9;
-                    q9 = o - 9 * s;
-                } else {
-                    const int pp = o / (3 * LL), rem = o - 3 * LL * pp;
-                    s = rem / 3;
-                    q9 = 3 * pp + (rem - 3 * s);
-                }
-                double val = smem_value(acc[s], q9);
-                if (has_diag && s == sd && (q9 % 4 == 0) && ((fixed_bits >> (q9 / 4)) & 1u)) val = 1e20;
+            auto put = [&](int s_, int q9, int64_t o) {
+                double val = smem_value(acc[s_], q9);
+                if (has_diag && s_ == sd && (q9 % 4 == 0) && ((fixed_bits >> (q9 / 4)) & 1u)) val = 1e20;
                 p.K[9 * rrs + o] = val;
+            };
+            if (p.k_layout == FEM_LAYOUT_BSR) {
+                for (int o = lane; o < 9 * LL; o += 32) {
+                    const int s_ = o / 9;
+                    put(s_, o - 9 * s_, o);
+                }
+            } else {
+                for (int pp = 0; pp < 3; ++pp)
+                    for (int idx = lane; idx < 3 * LL; idx += 32) {
+                        const int s_ = idx / 3;
+                        put(s_, 3 * pp + (idx - 3 * s_), int64_t(3 * LL) * pp + idx);
+                    }
             }
         }
         if (p.M) {
-            const int nm = p.m_layout == FEM_LAYOUT_BSR ? LL : 3 * LL;
-            for (int o = lane; o < nm; o += 32) {
-                const int s = p.m_layout == FEM_LAYOUT_BSR ? o : o % LL;
-                p.M[(p.m_layout == FEM_LAYOUT_BSR ? rrs : 3 * rrs) + o] = smem_value(acc[s], 9);
+            if (p.m_layout == FEM_LAYOUT_BSR) {
+                for (int o = lane; o < LL; o += 32) p.M[rrs + o] = smem_value(acc[o], 9);
+            } else {
+                for (int o = lane; o < LL; o += 32) {
+                    const double mv = smem_value(acc[o], 9);
+                    p.M[3 * rrs + o] = mv;
+                    p.M[3 * rrs + LL + o] = mv;
+                    p.M[3 * rrs + 2 * LL + o] = mv;
+                }
             }
         }
     }
@@ -509,12 +556,15 @@ void split_host(double x, float2& out) {
 
 }  // namespace
 
-int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st) {
+int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st,
+                           int64_t e_begin, int64_t e_end) {
+    if (e_end <= e_begin) return FEM_OK;
     ElemDdParams ep;
     ep.xyz = mesh->xyz;
     ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
     ep.ne_inv = mesh->ne_inv;
-    ep.n_elem = mesh->n_elem;
+    ep.e_begin = e_begin;
+    ep.e_end = e_end;
     ep.rec = static_cast<float2*>(workspace);
     const double EX = mat->EX, PO = mat->PO;
     const double D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // FEM_model_bsr.py:435-437
@@ -542,15 +592,18 @@ int launch_hex8_element_dd(const fem_mesh* mesh, const fem_material* mat, void* 
             for (int g = 0; g < 8; ++g) split_host(T.nr[g][a] * T.nr[g][b2], ep.tab.nn[pair_index(a, b2)][g]);
     const size_t smem = sizeof(ElemDdSmem);
     FEM_CUDA(cudaFuncSetAttribute(k_hex8_element_dd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
+    const int64_t blocks = (e_end - e_begin + kEpc - 1) / kEpc;
     k_hex8_element_dd<<<unsigned(blocks), kElemThreads, smem, st>>>(ep);
     FEM_LAUNCH_CHECK("k_hex8_element_dd");
     return FEM_OK;
 }
 
-int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st) {
+int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st,
+                     int64_t row_begin, int64_t row_end) {
+    if (row_end <= row_begin) return FEM_OK;
     GatherDdParams gp;
-    gp.n_node = mesh->n_node;
+    gp.row_begin = row_begin;
+    gp.row_end = row_end;
     gp.indptr = mesh->indptr;
     gp.indices = mesh->indices;
     gp.ne_ptr = mesh->ne_ptr;
@@ -566,7 +619,7 @@ int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const vo
     const size_t smem = sizeof(GatherDdSmem);
     FEM_CUDA(cudaFuncSetAttribute(k_gather_dd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t rows_per_cta = int64_t(kGWarps) * kRowsPerWarp;
-    const int64_t blocks = (mesh->n_node + rows_per_cta - 1) / rows_per_cta;
+    const int64_t blocks = (row_end - row_begin + rows_per_cta - 1) / rows_per_cta;
     k_gather_dd<<<unsigned(blocks), kGWarps * 32, smem, st>>>(gp);
     FEM_LAUNCH_CHECK("k_gather_dd");
     return FEM_OK;

@@ -239,3 +239,33 @@ extern "C" int fem_gather_map(int64_t n_node, int64_t n_elem, const int32_t* con
     }
     return FEM_OK;
 }
+
+extern "C" int fem_pipeline_plan(int64_t n_node, int64_t n_elem, const int32_t* indptr, const int32_t* ne_ptr,
+                                 const int32_t* ne_list, int n_parts, int64_t* row_split, int64_t* elem_split,
+                                 int64_t* block_split) {
+    FEM_REQUIRE(n_node >= 0 && n_elem >= 0, "negative size");
+    FEM_REQUIRE(n_parts >= 1 && n_parts <= 4096, "n_parts must lie in [1, 4096]");
+    FEM_REQUIRE(row_split && elem_split && block_split, "NULL output");
+    FEM_REQUIRE(n_node == 0 || (indptr && ne_ptr && (n_elem == 0 || ne_list)), "NULL pattern/incidence array");
+    const int64_t nnzb = n_node ? indptr[n_node] : 0;
+    // rows split so that every part holds about the same number of blocks (copy volume)
+    row_split[0] = 0;
+    for (int q = 1; q < n_parts; ++q) {
+        const int64_t target = nnzb * q / n_parts;
+        const int32_t* it = std::lower_bound(indptr, indptr + n_node + 1, int32_t(target));
+        row_split[q] = std::max(row_split[q - 1], int64_t(it - indptr));
+        row_split[q] = std::min<int64_t>(row_split[q], n_node);
+    }
+    row_split[n_parts] = n_node;
+    // elements a part needs: every element incident to one of its rows or an earlier row
+    int64_t emax = 0;
+    int64_t r = 0;
+    elem_split[0] = 0;
+    for (int q = 1; q <= n_parts; ++q) {
+        for (; r < row_split[q]; ++r)
+            if (ne_ptr[r + 1] > ne_ptr[r]) emax = std::max<int64_t>(emax, (ne_list[ne_ptr[r + 1] - 1] >> 3) + 1);
+        elem_split[q] = q == n_parts ? n_elem : std::min(emax, n_elem);
+    }
+    for (int q = 0; q <= n_parts; ++q) block_split[q] = n_node ? indptr[row_split[q]] : 0;
+    return FEM_OK;
+}

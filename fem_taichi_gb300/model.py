@@ -8,9 +8,10 @@ reference's constructor and getters:
     Get_VectorF()                   -> ndarray (3N,), node-major
 
 All arithmetic runs in the sm_103a kernels of ``libfemgb.so``; mesh, pattern and outputs
-live in HBM (torch tensors used as raw device buffers).  Getters are idempotent: each call
-recomputes from scratch, whereas the reference's Taichi fields accumulate across repeated
-calls (FEM_model_bsr.py:174; values match the reference's first call).
+live in HBM (torch tensors used as raw device buffers).  The getters share one assembly pass
+(``fem_assemble_host``) whose device->host copies of each part of the block rows overlap the
+kernels of the next part.  Getters are idempotent: the reference's Taichi fields accumulate
+across repeated calls (FEM_model_bsr.py:174; values match the reference's first call).
 
 Extensions beyond the reference surface (for the solver and the benchmark):
     assemble(k_layout, m_layout)  -> device tensors (K, M, F) without host copies
@@ -134,7 +135,9 @@ class Model:
         self._ws = None
         self._csr_index = None
         self._version = 0          # bumped whenever an assembly input changes
-        self._cache = None         # (version, K_csr, M_csr, F) device tensors of the last assembly
+        self._cache = None         # (version, {"K", "M", "F"} host arrays not yet handed out)
+        self._plan = None
+        self.pipeline_parts = 8    # parts of fem_assemble_host (copies overlap the next part)
         if algo not in ("dd", "fp64"):
             raise ValueError("algo must be 'dd' or 'fp64'")
         self.algo = algo
@@ -193,47 +196,79 @@ class Model:
             self._csr_index = tuple(t.cpu().numpy() for t in (rowK, colK, rowM, colM))
         return self._csr_index
 
-    @staticmethod
-    def _to_host(t: torch.Tensor) -> np.ndarray:
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        h.copy_(t, non_blocking=True)
-        torch.cuda.current_stream(t.device).synchronize()
-        return h.numpy()
+    def pipeline_plan(self, n_parts=None):
+        """(row_split, elem_split, block_split) int64 host arrays of fem_assemble_host (cached)."""
+        n_parts = self.pipeline_parts if n_parts is None else int(n_parts)
+        if self._plan is None or self._plan[0] != n_parts:
+            P = self.Physics
+            ind = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+            nep = np.ascontiguousarray(P.ne_ptr, dtype=np.int32)
+            nel = np.ascontiguousarray(P.ne_list, dtype=np.int32)
+            rs, es, bs = (np.zeros(n_parts + 1, dtype=np.int64) for _ in range(3))
+            _lib.check(self.lib.fem_pipeline_plan(self.Num_Node, self.Num_Elem, ind.ctypes.data, nep.ctypes.data,
+                                                  nel.ctypes.data, n_parts, rs.ctypes.data, es.ctypes.data,
+                                                  bs.ctypes.data), "fem_pipeline_plan")
+            self._plan = (n_parts, rs, es, bs)
+        return self._plan[1:]
+
+    def assemble_host(self, n_parts=None):
+        """One assembly pass delivered to page-locked host arrays: K (9*nnzb,) and M (3*nnzb,)
+        in the reference CSR orders, F (3N,).  The device->host copies of each part of the
+        block rows overlap the kernels of the next part (fem_assemble_host)."""
+        d = self.device
+        nnzb = self.mesh.nnzb
+        Kd = torch.empty(9 * nnzb, dtype=torch.float64, device=d)
+        Md = torch.empty(3 * nnzb, dtype=torch.float64, device=d)
+        Fd = torch.empty((self.Num_Node, 3), dtype=torch.float64, device=d)
+        Kh = torch.empty(9 * nnzb, dtype=torch.float64, pin_memory=True)
+        Mh = torch.empty(3 * nnzb, dtype=torch.float64, pin_memory=True)
+        Fh = torch.empty(3 * self.Num_Node, dtype=torch.float64, pin_memory=True)
+        ws = self.workspace()
+        o = FemAssemblyOut(LAYOUT_CSR, LAYOUT_CSR, Kd.data_ptr(), Md.data_ptr(), Fd.data_ptr(),
+                           self.fixed.data_ptr(), self.loads.data_ptr(),
+                           _lib.ALGO_DD if self.algo == "dd" else _lib.ALGO_FP64)
+        rs, es, bs = self.pipeline_plan(n_parts)
+        _lib.check(self.lib.fem_assemble_host(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), ctypes.byref(o),
+                                              rs.ctypes.data, es.ctypes.data, bs.ctypes.data, len(rs) - 1,
+                                              Kh.data_ptr(), Mh.data_ptr(), Fh.data_ptr(), _dptr(ws), ws.numel(),
+                                              _stream(d)), "fem_assemble_host")
+        torch.cuda.current_stream(d).synchronize()
+        return Kh.numpy(), Mh.numpy(), Fh.numpy()
 
     def set_coordinates(self, xyz) -> None:
         """Move the nodes (same topology); the next getter re-assembles."""
         self.mesh.set_coordinates(xyz)
         self._version += 1
 
-    def _assembled(self):
-        """K, M (reference CSR orders) and F from one assembly pass, reused by the three
-        getters until an input changes (the element integrals are shared)."""
-        if self._cache is None or self._cache[0] != self._version:
-            K, M, F = self.assemble(k_layout="csr", m_layout="csr")
-            self._cache = (self._version, K, M, F)
-        return self._cache[1:]
+    def _take(self, key):
+        """Host result `key` of the current inputs.  One assembly pass serves K, M and F;
+        each array is handed out once (a repeated getter call runs a new pass, so callers
+        never share a buffer)."""
+        if self._cache is None or self._cache[0] != self._version or key not in self._cache[1]:
+            K, M, F = self.assemble_host()
+            self._cache = (self._version, {"K": K, "M": M, "F": F})
+        return self._cache[1].pop(key)
 
     # -- reference getters -------------------------------------------------------------
     def Get_MatrixKL(self):
         """FEM_model_csr.py:118-127: K as scipy CSR (penalty applied)."""
-        K, _, _ = self._assembled()
+        K = self._take("K")
         rowK, colK, _, _ = self.csr_index()
         n = self.Num_Free
-        return sp.csr_matrix((self._to_host(K), colK, rowK), shape=(n, n), dtype=np.float64)
+        return sp.csr_matrix((K, colK, rowK), shape=(n, n), dtype=np.float64, copy=False)
 
     Get_MatrixK = Get_MatrixKL
 
     def Get_MatrixM(self):
         """FEM_model_csr.py:129-137 / FEM_model_bsr.py:147-155."""
-        _, M, _ = self._assembled()
+        M = self._take("M")
         _, _, rowM, colM = self.csr_index()
         n = self.Num_Free
-        return sp.csr_matrix((self._to_host(M), colM, rowM), shape=(n, n), dtype=np.float64)
+        return sp.csr_matrix((M, colM, rowM), shape=(n, n), dtype=np.float64, copy=False)
 
     def Get_VectorF(self):
         """FEM_model_csr.py:141-146: element centrifugal loads + nodal loads, node-major (3N,)."""
-        _, _, F = self._assembled()
-        return self._to_host(F).reshape(-1).copy()
+        return self._take("F")
 
     def Get_MatrixKN(self):
         raise NotImplementedError("large-displacement tangent (FEM_model_bsr.py:134-145) is not built")

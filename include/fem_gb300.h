@@ -121,6 +121,28 @@ int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int alg
 int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* Assembly delivered to host memory: replaces the reference getters' "run the kernels, then
+ * to_numpy()" (Get_MatrixKL / Get_MatrixM / Get_VectorF, FEM_model_csr.py:118-146).  The
+ * mesh is assembled in n_parts parts of consecutive block rows; part q's rows are copied
+ * from the device outputs in `out` to K_host / M_host / F_host (same layouts as out; NULL
+ * skips one) on an internal copy stream while later parts still compute, so the copies
+ * overlap the kernels.  The plan comes from fem_pipeline_plan.  Host buffers may be
+ * page-locked (copies asynchronous) or pageable (copies then finish before the call
+ * returns).  `stream` is ordered after the last copy: synchronise it before reading the host
+ * buffers.  Not capturable into a CUDA graph.  FEM_ALGO_FP64 runs as a single part. */
+int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                      const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
+                      int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
+                      size_t workspace_bytes, void* stream);
+/* Plan of fem_assemble_host (host arrays, no reference counterpart): row_split[0..n_parts]
+ * splits the block rows into parts of about nnzb / n_parts blocks; block_split[q] =
+ * indptr[row_split[q]]; elem_split[q + 1] = 1 + the largest element incident to a row below
+ * row_split[q + 1] (prefix maximum), so part q computes elements [elem_split[q],
+ * elem_split[q+1]) and then gathers its rows.  indptr, ne_ptr, ne_list: host copies. */
+int fem_pipeline_plan(int64_t n_node, int64_t n_elem, const int32_t* indptr, const int32_t* ne_ptr,
+                      const int32_t* ne_list, int n_parts, int64_t* row_split, int64_t* elem_split,
+                      int64_t* block_split);
+
 /* Reference CSR index arrays (depend on the pattern only): rowK [3N+1], colK [9 nnzb],
  * rowM [3N+1], colM [3 nnzb]; any may be NULL. */
 int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* rowM,

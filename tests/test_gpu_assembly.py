@@ -158,3 +158,60 @@ def test_full_size_c2_against_c_oracle(algo, c2_oracle):
     assert_vec_close(Fd.cpu().numpy(), Fc)
     # total mass = rho * volume (sum_g detJ), a size-independent invariant
     assert abs(Md.sum().item() - STEEL['DE'] * 200 * 200 * 24) <= 1e-10 * STEEL['DE'] * 200 * 200 * 24
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("order", ["natural", "shuffled"])
+def test_host_pipeline_equals_device_assembly(algo, order):
+    """fem_assemble_host (parts of block rows, copies overlapping later parts) returns the
+    device assembly bit for bit, for any number of parts, into page-locked or pageable
+    host memory."""
+    import ctypes
+    from fem_taichi_gb300 import _lib
+    from fem_taichi_gb300.model import _dptr, _stream
+    P = F.hex_block(13, 9, 5, jitter=0.1, seed=6, fix="zmin")
+    if order == "shuffled":
+        perm = np.random.default_rng(2).permutation(P.Num_Elem)
+        P = F.Physics(P.Node[0], P.xyz, P.conn[perm].T, P.Bounds, [])
+    M = F.Model("h", P, STEEL, algo=algo)
+    Kd, Md, Fd = M.assemble(k_layout="csr", m_layout="csr")
+    torch.cuda.synchronize()
+    Kd, Md, Fd = Kd.cpu().numpy(), Md.cpu().numpy(), Fd.cpu().numpy().reshape(-1)
+    for parts in (1, 3, 8, 50):
+        Kh, Mh, Fh = M.assemble_host(parts)
+        assert np.array_equal(Kh, Kd) and np.array_equal(Mh, Md) and np.array_equal(Fh, Fd)
+    # pageable destination (plain numpy arrays)
+    L = _lib.load()
+    nnzb = M.mesh.nnzb
+    Kt = torch.empty(9 * nnzb, dtype=torch.float64, device="cuda")
+    Mt = torch.empty(3 * nnzb, dtype=torch.float64, device="cuda")
+    Ft = torch.empty(3 * P.Num_Node, dtype=torch.float64, device="cuda")
+    Kp, Mp, Fp = np.full(9 * nnzb, np.nan), np.full(3 * nnzb, np.nan), np.full(3 * P.Num_Node, np.nan)
+    o = _lib.FemAssemblyOut(_lib.LAYOUT_CSR, _lib.LAYOUT_CSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
+                            M.fixed.data_ptr(), M.loads.data_ptr(), _lib.ALGO_DD if algo == "dd" else _lib.ALGO_FP64)
+    rs, es, bs = M.pipeline_plan(4)
+    ws = M.workspace()
+    _lib.check(L.fem_assemble_host(ctypes.byref(M.mesh.c), ctypes.byref(M.mat), ctypes.byref(o), rs.ctypes.data,
+                                   es.ctypes.data, bs.ctypes.data, 4, Kp.ctypes.data, Mp.ctypes.data, Fp.ctypes.data,
+                                   _dptr(ws), ws.numel(), _stream(M.device)))
+    torch.cuda.synchronize()
+    assert np.array_equal(Kp, Kd) and np.array_equal(Mp, Md) and np.array_equal(Fp, Fd)
+
+
+def test_host_pipeline_rejects_bad_plan():
+    import ctypes
+    from fem_taichi_gb300 import _lib
+    from fem_taichi_gb300.model import _dptr, _stream
+    P = F.hex_block(3, 3, 2)
+    M = F.Model("b", P, STEEL)
+    rs, es, bs = (a.copy() for a in M.pipeline_plan(2))
+    rs[1], rs[2] = rs[2], rs[1]          # not monotone
+    Kt = torch.empty(9 * M.mesh.nnzb, dtype=torch.float64, device="cuda")
+    o = _lib.FemAssemblyOut(_lib.LAYOUT_CSR, _lib.LAYOUT_CSR, Kt.data_ptr(), None, None, None, None, _lib.ALGO_DD)
+    Kh = np.zeros(9 * M.mesh.nnzb)
+    ws = M.workspace()
+    L = _lib.load()
+    rc = L.fem_assemble_host(ctypes.byref(M.mesh.c), ctypes.byref(M.mat), ctypes.byref(o), rs.ctypes.data,
+                             es.ctypes.data, bs.ctypes.data, 2, Kh.ctypes.data, None, None, _dptr(ws), ws.numel(),
+                             _stream(M.device))
+    assert rc == _lib.FEM_ERR_INVALID

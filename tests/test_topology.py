@@ -91,3 +91,42 @@ def test_gather_map_matches_search():
         cols = P.conn[e, b]
         s = P.slot_map.reshape(-1, 8)[k, b].astype(np.int64)
         assert np.array_equal(P.ReNode[P.SmNode[rows] + s], cols)
+
+
+def _plan(P, parts):
+    L = _lib.load()
+    ind = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+    nep = np.ascontiguousarray(P.ne_ptr, dtype=np.int32)
+    nel = np.ascontiguousarray(P.ne_list, dtype=np.int32)
+    rs, es, bs = (np.zeros(parts + 1, dtype=np.int64) for _ in range(3))
+    _lib.check(L.fem_pipeline_plan(P.Num_Node, P.Num_Elem, ind.ctypes.data, nep.ctypes.data, nel.ctypes.data,
+                                   parts, rs.ctypes.data, es.ctypes.data, bs.ctypes.data))
+    return rs, es, bs
+
+
+@pytest.mark.parametrize("parts", [1, 2, 8, 37])
+@pytest.mark.parametrize("order", ["natural", "shuffled"])
+def test_pipeline_plan(parts, order):
+    """Every row of part q only needs elements below elem_split[q+1]; splits span the mesh
+    monotonically; block_split = indptr[row_split]; parts hold about nnzb / parts blocks."""
+    P = F.hex_block(9, 7, 5, jitter=0.1, seed=3)
+    if order == "shuffled":
+        perm = np.random.default_rng(1).permutation(P.Num_Elem)
+        P = F.Physics(P.Node[0], P.xyz, P.conn[perm].T, [], [])
+    rs, es, bs = _plan(P, parts)
+    assert rs[0] == 0 and rs[-1] == P.Num_Node and es[0] == 0 and es[-1] == P.Num_Elem
+    assert np.all(np.diff(rs) >= 0) and np.all(np.diff(es) >= 0) and np.all(np.diff(bs) >= 0)
+    assert np.array_equal(bs, P.SmNode[rs])
+    for q in range(parts):
+        for r in range(rs[q], rs[q + 1]):
+            inc = P.ne_list[P.ne_ptr[r]:P.ne_ptr[r + 1]] >> 3
+            assert inc.size == 0 or inc.max() < es[q + 1]
+    nnzb = int(P.SmNode[-1])
+    maxrow = int(np.diff(P.SmNode).max())
+    assert np.all(np.abs(np.diff(bs) - nnzb / parts) <= maxrow + 1)
+
+
+def test_pipeline_plan_rejects_bad_parts():
+    P = F.hex_block(2, 2, 2)
+    with pytest.raises(_lib.FemError):
+        _plan(P, 0)
