@@ -430,12 +430,15 @@ __device__ void gather_row_long(const GatherDdParams& p, int64_t row, int lane) 
     }
 }
 
+// kRanged: the launch covers rows [row_begin, row_end) (one part of a split assembly); the
+// whole-mesh launch (row_begin == 0) keeps the simpler index arithmetic of kRanged == false.
+template <bool kRanged>
 __global__ void __launch_bounds__(kGWarps * 32) k_gather_dd(const GatherDdParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GatherDdSmem& S = *reinterpret_cast<GatherDdSmem*>(smem_raw);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = lane >> 3, b = lane & 7;
-    const int64_t row0 = p.row_begin + (int64_t(blockIdx.x) * kGWarps + w) * kRowsPerWarp;
+    const int64_t row0 = (kRanged ? p.row_begin : 0) + (int64_t(blockIdx.x) * kGWarps + w) * kRowsPerWarp;
     if (row0 >= p.row_end) return;
     const int64_t row = row0 + r;
     const bool vrow = row < p.row_end;
@@ -617,10 +620,15 @@ int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const vo
     gp.fixed = out->fixed;
     gp.loads = out->loads;
     const size_t smem = sizeof(GatherDdSmem);
-    FEM_CUDA(cudaFuncSetAttribute(k_gather_dd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t rows_per_cta = int64_t(kGWarps) * kRowsPerWarp;
     const int64_t blocks = (row_end - row_begin + rows_per_cta - 1) / rows_per_cta;
-    k_gather_dd<<<unsigned(blocks), kGWarps * 32, smem, st>>>(gp);
+    if (row_begin == 0) {
+        FEM_CUDA(cudaFuncSetAttribute(k_gather_dd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        k_gather_dd<false><<<unsigned(blocks), kGWarps * 32, smem, st>>>(gp);
+    } else {
+        FEM_CUDA(cudaFuncSetAttribute(k_gather_dd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        k_gather_dd<true><<<unsigned(blocks), kGWarps * 32, smem, st>>>(gp);
+    }
     FEM_LAUNCH_CHECK("k_gather_dd");
     return FEM_OK;
 }

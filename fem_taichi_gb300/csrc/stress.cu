@@ -216,6 +216,7 @@ extern "C" int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, cons
         return FEM_ERR_WORKSPACE;
     }
     FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
+    FEM_REQUIRE(workspace == nullptr || aligned16(workspace), "workspace not 16-byte aligned");
     cudaStream_t st = as_stream(stream);
     if (algo == FEM_ALGO_DD) return launch_stress_dd(mesh, mat, u, co_elem, extrap, out, workspace, st);
     if (mesh->n_elem) {
@@ -312,7 +313,8 @@ struct StressDdParams {
     const int4* conn4;
     const double* u;
     int64_t n_elem;
-    float2* rec;  // [n_elem][8][6] float pairs
+    const int32_t* ne_inv;  // NULL: record of (e, j) at e*8+j; else at ne_inv[e*8+j] (row order)
+    float2* rec;            // 8 * n_elem records of 6 float pairs
     float2 D0d, lam, mu;
     float2 dnr[8][8][3];
     float2 W[8][8];
@@ -351,20 +353,38 @@ __global__ void __launch_bounds__(kThreads) k_stress_element_dd(const StressDdPa
     if (valid) {
         const int g = t;
         dd J[3][3], G[3][3];
+        {
+            dd_acc aj[3][3], ag[3][3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+            for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                dd_acc aj = acc_zero(), ag = acc_zero();
+                for (int d = 0; d < 3; ++d) aj[i][d] = ag[i][d] = acc_zero();
+            // corner loop kept rolled: the unrolled form overflows the instruction cache
+#pragma unroll 1
+            for (int a = 0; a < 8; ++a) {
+                dd c[3], xa[3], ua[3];
 #pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    const dd c = ldp(s.dnr[g][a][d]);
-                    acc_fma(aj, ldp(s.x[el][a][i]), c);
-                    acc_fma(ag, ldp(s.u[el][a][i]), c);
+                for (int i = 0; i < 3; ++i) {
+                    c[i] = ldp(s.dnr[g][a][i]);
+                    xa[i] = ldp(s.x[el][a][i]);
+                    ua[i] = ldp(s.u[el][a][i]);
                 }
-                J[i][d] = acc_value(aj);
-                G[i][d] = acc_value(ag);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        acc_fma(aj[i][d], xa[i], c[d]);
+                        acc_fma(ag[i][d], ua[i], c[d]);
+                    }
             }
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    J[i][d] = acc_value(aj[i][d]);
+                    G[i][d] = acc_value(ag[i][d]);
+                }
+        }
         dd A[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -408,14 +428,19 @@ __global__ void __launch_bounds__(kThreads) k_stress_element_dd(const StressDdPa
     __syncthreads();
     if (!valid) return;
     const int j = t;
-    float2* o = p.rec + (e * 8 + j) * 6;
+    const int64_t slot = p.ne_inv ? int64_t(__ldg(p.ne_inv + e * 8 + j)) : e * 8 + j;
+    float2* o = p.rec + slot * 6;
+    dd_acc acc[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        dd_acc acc = acc_zero();
+    for (int c = 0; c < 6; ++c) acc[c] = acc_zero();
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+        const dd w = ldp(s.W[j][k]);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) acc_fma(acc, ldp(s.W[j][k]), ldp(s.sv[el][k][c]));
-        o[c] = stp(acc_value(acc));
+        for (int c = 0; c < 6; ++c) acc_fma(acc[c], w, ldp(s.sv[el][k][c]));
     }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o[c] = stp(acc_value(acc[c]));
 }
 
 // Cyclic Jacobi on a symmetric 3x3 in double-float; returns the eigenvalues descending.
@@ -467,7 +492,8 @@ __device__ void sym3_eig_desc_dd(dd (&a)[3][3], dd& p1, dd& p2, dd& p3) {
 __global__ void __launch_bounds__(256) k_stress_node_dd(int64_t n_node, const int32_t* __restrict__ ne_ptr,
                                                         const int32_t* __restrict__ ne_list,
                                                         const int32_t* __restrict__ co_elem,
-                                                        const float2* __restrict__ rec, double* __restrict__ out) {
+                                                        const float2* __restrict__ rec, int row_ordered,
+                                                        double* __restrict__ out) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n_node) return;
     dd_acc acc[6];
@@ -475,10 +501,18 @@ __global__ void __launch_bounds__(256) k_stress_node_dd(int64_t n_node, const in
     for (int c = 0; c < 6; ++c) acc[c] = acc_zero();
     const int ks = ne_ptr[i], ke = ne_ptr[i + 1];
     for (int k = ks; k < ke; ++k) {
-        const int ent = __ldg(ne_list + k);
-        const float2* r = rec + (int64_t(ent >> 3) * 8 + (ent & 7)) * 6;
+        int64_t slot = k;  // row order: this node's corner records are contiguous
+        if (!row_ordered) {
+            const int ent = __ldg(ne_list + k);
+            slot = int64_t(ent >> 3) * 8 + (ent & 7);
+        }
+        const float4* r = reinterpret_cast<const float4*>(rec + slot * 6);  // 48 bytes, 16-byte aligned
 #pragma unroll
-        for (int c = 0; c < 6; ++c) acc_add(acc[c], ldp(__ldg(r + c)));
+        for (int q = 0; q < 3; ++q) {
+            const float4 v = __ldg(r + q);
+            acc_add(acc[2 * q], dd{v.x, v.y});
+            acc_add(acc[2 * q + 1], dd{v.z, v.w});
+        }
     }
     double* o = out + 10 * i;
     const int ce = co_elem[i];
@@ -522,6 +556,7 @@ int launch_stress_dd(const fem_mesh* mesh, const fem_material* mat, const double
         sp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
         sp.u = u;
         sp.n_elem = mesh->n_elem;
+        sp.ne_inv = mesh->ne_inv;
         sp.rec = static_cast<float2*>(workspace);
         const double EX = mat->EX, PO = mat->PO;
         split2(EX * (1 - PO) / (1 + PO) / (1 - 2 * PO), sp.D0d);  // POST_process.py:292-302
@@ -539,7 +574,8 @@ int launch_stress_dd(const fem_mesh* mesh, const fem_material* mat, const double
     }
     const int64_t blocks = (mesh->n_node + 255) / 256;
     k_stress_node_dd<<<unsigned(blocks), 256, 0, st>>>(mesh->n_node, mesh->ne_ptr, mesh->ne_list, co_elem,
-                                                       static_cast<const float2*>(workspace), out);
+                                                       static_cast<const float2*>(workspace),
+                                                       mesh->ne_inv != nullptr, out);
     FEM_LAUNCH_CHECK("k_stress_node_dd");
     return FEM_OK;
 }

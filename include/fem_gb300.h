@@ -157,7 +157,9 @@ int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
                const int32_t* co_elem, const double* extrap, double* out, void* workspace,
                size_t workspace_bytes, void* stream);
 /* fem_stress with the arithmetic chosen: FEM_ALGO_DD (double-float on the FP32 pipes, what
- * fem_stress uses) or FEM_ALGO_FP64 (native FP64). */
+ * fem_stress uses) or FEM_ALGO_FP64 (native FP64).  With mesh->ne_inv set, FEM_ALGO_DD keeps
+ * each node's corner records contiguous in the workspace (faster node pass); without it the
+ * records stay in element order.  Same results either way.  workspace: 16-byte aligned. */
 int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, const double* u,
                   const int32_t* co_elem, const double* extrap, double* out, void* workspace,
                   size_t workspace_bytes, int algo, void* stream);

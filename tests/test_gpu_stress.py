@@ -73,3 +73,24 @@ def test_double_eigenvalues_and_constant_fields():
         for algo in ("dd", "fp64"):
             S = F.Post("p", P, STEEL, u, algo=algo).Get_Stress()
             assert_stress_close(S, O.oracle_stress(P, STEEL, u))
+
+
+def test_row_ordered_and_element_ordered_records_agree():
+    """FEM_ALGO_DD stress with and without mesh->ne_inv (row-ordered vs element-ordered
+    corner records) gives the same bits."""
+    import ctypes
+    import torch
+    P = F.hex_block(9, 7, 4, jitter=0.12, seed=5)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-1e-3, 1e-3, size=(P.Num_Node, 3))
+    post = F.Post("r", P, STEEL, u)
+    a = post.stress_device().clone()
+    c = post.mesh.c
+    saved = c.ne_inv
+    try:
+        c.ne_inv = None
+        b = post.stress_device().clone()
+    finally:
+        c.ne_inv = saved
+    torch.cuda.synchronize()
+    assert torch.equal(torch.nan_to_num(a), torch.nan_to_num(b))
