@@ -30,6 +30,7 @@ FEM_ERR_BREAKDOWN = -8
 LAYOUT_BSR = 0
 LAYOUT_CSR = 1
 LAYOUT_RSOA = 2
+LAYOUT_RSOA4 = 3
 ALGO_DD = 0
 ALGO_FP64 = 1
 FEM_F64 = 0
@@ -103,6 +104,8 @@ SIGNATURES = {
     "fem_assemble_host": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), ctypes.POINTER(FemAssemblyOut),
                                   c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_size_t, c_void_p]),
+    "fem_rsoa4_indptr": (c_int, [c_int64, c_void_p, c_void_p]),
+    "fem_bsr_to_rsoa4_f32": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_pipeline_plan": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                   c_void_p]),
     "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -467,7 +467,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
     PcgState* st = reinterpret_cast<PcgState*>(ws + L.state);
     double* part = reinterpret_cast<double*>(ws + L.part);
     BsrView<double> K64{n, A64->indptr, A64->indices, static_cast<const double*>(A64->vals),
-                        A64->layout == FEM_LAYOUT_RSOA};
+                        rsoa_kind(A64->layout)};
     const int maxit = std::max(1, o->maxit);
     InnerResult ir{0, FEM_OK};
     PcgState h;
@@ -510,7 +510,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
         if (rc) return rc;
     } else {
         BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
-                           A32->layout == FEM_LAYOUT_RSOA};
+                           rsoa_kind(A32->layout)};
         double* y = reinterpret_cast<double*>(ws + L.v64[0]);
         double* r64 = reinterpret_cast<double*>(ws + L.v64[1]);
         float* b32 = reinterpret_cast<float*>(ws + L.v32[0]);
@@ -596,12 +596,19 @@ extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const doubl
     FEM_REQUIRE(A64 && opts && stats && precond && F && U, "NULL argument");
     FEM_REQUIRE(A64->dtype == FEM_F64 && A64->n_brow > 0 && A64->indptr && A64->indices && A64->vals,
                 "A64 must be a non-empty FP64 BSR matrix");
+    FEM_REQUIRE(A64->layout == FEM_LAYOUT_BSR || A64->layout == FEM_LAYOUT_RSOA, "A64: layout must be BSR or RSOA");
     const int R = opts->nrhs;
     FEM_REQUIRE(R == 1 || R == 2 || R == 4 || R == 8 || R == 16 || R == 32, "nrhs must be 1, 2, 4, 8, 16 or 32");
     FEM_REQUIRE(opts->rtol > 0 && opts->maxit > 0, "rtol and maxit must be positive");
     if (opts->mixed) {
-        FEM_REQUIRE(A32 && A32->dtype == FEM_F32 && A32->n_brow == A64->n_brow && A32->vals,
+        FEM_REQUIRE(A32 && A32->dtype == FEM_F32 && A32->n_brow == A64->n_brow && A32->vals && A32->indptr &&
+                        A32->indices,
                     "mixed precision needs the FP32 copy of the matrix (A32)");
+        FEM_REQUIRE(A32->layout == FEM_LAYOUT_BSR || A32->layout == FEM_LAYOUT_RSOA || A32->layout == FEM_LAYOUT_RSOA4,
+                    "A32: layout must be BSR, RSOA or RSOA4");
+        FEM_REQUIRE(A32->layout != FEM_LAYOUT_RSOA4 ||
+                        ((reinterpret_cast<uintptr_t>(A32->vals) | reinterpret_cast<uintptr_t>(A32->indices)) & 15u) == 0,
+                    "A32: FEM_LAYOUT_RSOA4 arrays must be 16-byte aligned");
         FEM_REQUIRE(opts->inner_rtol > 0 && opts->inner_rtol < 1, "inner_rtol must lie in (0, 1)");
     }
     const Layout L = layout(A64->n_brow, R, opts->mixed);

@@ -42,6 +42,27 @@ __global__ void __launch_bounds__(256) k_bsr_to_rsoa_f32(int64_t n, const int32_
     }
 }
 
+// BSR [nnzb][9] FP64 -> padded row-SoA FP32 (rows rounded up to 4 blocks; padding: column
+// = the row itself, values 0)
+__global__ void __launch_bounds__(256) k_bsr_to_rsoa4_f32(int64_t n, const int32_t* __restrict__ indptr,
+                                                          const int32_t* __restrict__ indices,
+                                                          const double* __restrict__ src,
+                                                          const int32_t* __restrict__ indptr4, int32_t* indices4,
+                                                          float* __restrict__ dst) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = warp0; i < n; i += nw) {
+        const int64_t rs = indptr[i], rs4 = indptr4[i];
+        const int L = indptr[i + 1] - int(rs), Lp = indptr4[i + 1] - int(rs4);
+        for (int l = lane; l < Lp; l += 32) indices4[rs4 + l] = l < L ? indices[rs + l] : int32_t(i);
+        for (int o = lane; o < 9 * Lp; o += 32) {
+            const int q = o / Lp, l = o - q * Lp;
+            dst[9 * rs4 + o] = l < L ? float(src[9 * (rs + l) + q]) : 0.f;
+        }
+    }
+}
+
 __global__ void k_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
         dst[i] = float(src[i]);
@@ -126,7 +147,12 @@ int check_bsr(const fem_bsr* A) {
     FEM_REQUIRE(A != nullptr, "A is NULL");
     FEM_REQUIRE(A->n_brow >= 0 && A->nnzb >= 0, "negative size");
     FEM_REQUIRE(A->dtype == FEM_F64 || A->dtype == FEM_F32, "dtype must be FEM_F64 or FEM_F32");
-    FEM_REQUIRE(A->layout == FEM_LAYOUT_BSR || A->layout == FEM_LAYOUT_RSOA, "layout must be BSR or RSOA");
+    FEM_REQUIRE(A->layout == FEM_LAYOUT_BSR || A->layout == FEM_LAYOUT_RSOA || A->layout == FEM_LAYOUT_RSOA4,
+                "layout must be BSR, RSOA or RSOA4");
+    FEM_REQUIRE(A->layout != FEM_LAYOUT_RSOA4 || A->dtype == FEM_F32, "FEM_LAYOUT_RSOA4 is FP32 only");
+    FEM_REQUIRE(A->layout != FEM_LAYOUT_RSOA4 || ((reinterpret_cast<uintptr_t>(A->vals) |
+                                                   reinterpret_cast<uintptr_t>(A->indices)) & 15u) == 0,
+                "FEM_LAYOUT_RSOA4 arrays must be 16-byte aligned");
     if (A->n_brow) FEM_REQUIRE(A->indptr != nullptr, "indptr is NULL");
     if (A->nnzb) FEM_REQUIRE(A->indices && A->vals, "indices/vals is NULL");
     return FEM_OK;
@@ -140,11 +166,11 @@ int bsr_spmv_any(const fem_bsr* A, int nrhs, const void* x, void* y, int variant
     if (A->n_brow == 0) return FEM_OK;
     if (A->dtype == FEM_F64) {
         BsrView<double> v{A->n_brow, A->indptr, A->indices, static_cast<const double*>(A->vals),
-                          A->layout == FEM_LAYOUT_RSOA};
+                          rsoa_kind(A->layout)};
         return launch_spmv<double>(v, nrhs, static_cast<const double*>(x), static_cast<double*>(y), variant, st);
     }
     BsrView<float> v{A->n_brow, A->indptr, A->indices, static_cast<const float*>(A->vals),
-                     A->layout == FEM_LAYOUT_RSOA};
+                     rsoa_kind(A->layout)};
     return launch_spmv<float>(v, nrhs, static_cast<const float*>(x), static_cast<float*>(y), variant, st);
 }
 
@@ -232,5 +258,35 @@ extern "C" int fem_bsr_to_rsoa_f32(const fem_bsr* A, float* dst, void* stream) {
     k_bsr_to_rsoa_f32<<<grid, 256, 0, as_stream(stream)>>>(A->n_brow, A->indptr, static_cast<const double*>(A->vals),
                                                            dst);
     FEM_LAUNCH_CHECK("k_bsr_to_rsoa_f32");
+    return FEM_OK;
+}
+
+extern "C" int fem_rsoa4_indptr(int64_t n_brow, const int32_t* indptr, int32_t* indptr4) {
+    FEM_REQUIRE(n_brow >= 0, "negative size");
+    FEM_REQUIRE(indptr && indptr4, "indptr/indptr4 is NULL");
+    int64_t acc = 0;
+    indptr4[0] = 0;
+    for (int64_t i = 0; i < n_brow; ++i) {
+        const int64_t L = int64_t(indptr[i + 1]) - indptr[i];
+        FEM_REQUIRE(L >= 0, "indptr is not monotone");
+        acc += (L + 3) / 4 * 4;
+        FEM_REQUIRE(acc < (int64_t(1) << 31), "padded block count exceeds int32 range");
+        indptr4[i + 1] = int32_t(acc);
+    }
+    return FEM_OK;
+}
+
+extern "C" int fem_bsr_to_rsoa4_f32(const fem_bsr* A, const int32_t* indptr4, int32_t* indices4, float* vals4,
+                                    void* stream) {
+    int rc = check_bsr(A);
+    if (rc) return rc;
+    FEM_REQUIRE(A->dtype == FEM_F64 && A->layout == FEM_LAYOUT_BSR, "source must be an FP64 BSR matrix");
+    if (A->n_brow == 0) return FEM_OK;
+    FEM_REQUIRE(indptr4 && indices4 && vals4, "indptr4/indices4/vals4 is NULL");
+    const unsigned grid = unsigned(std::min<int64_t>((A->n_brow + 7) / 8, int64_t(sm_count()) * 16));
+    k_bsr_to_rsoa4_f32<<<grid, 256, 0, as_stream(stream)>>>(A->n_brow, A->indptr, A->indices,
+                                                            static_cast<const double*>(A->vals), indptr4, indices4,
+                                                            vals4);
+    FEM_LAUNCH_CHECK("k_bsr_to_rsoa4_f32");
     return FEM_OK;
 }

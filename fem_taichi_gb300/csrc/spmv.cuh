@@ -20,8 +20,13 @@ struct BsrView {
     const int32_t* indptr;  // [n+1]
     const int32_t* indices; // [nnzb]
     const T* vals;          // [nnzb][3][3] (BSR) or, per block row, [9][row length] (row-SoA)
-    int rsoa;               // 1: row-SoA value layout
+    int rsoa;               // 1: row-SoA value layout; 2: row-SoA padded to 4-block multiples (FP32)
 };
+
+// BsrView::rsoa for a fem_bsr layout code
+inline int rsoa_kind(int layout) {
+    return layout == FEM_LAYOUT_RSOA ? 1 : layout == FEM_LAYOUT_RSOA4 ? 2 : 0;
+}
 
 // address of value q (0..8) of the block in slot l of the row starting at rs with L blocks
 template <typename T>
@@ -37,11 +42,67 @@ __device__ __forceinline__ V group_sum(V v) {
     return v;
 }
 
+// Padded row-SoA FP32 product: each lane takes 4 consecutive slots of its row per step and
+// reads each of the 9 values of those 4 blocks with one 16-byte load (rows, values and
+// slot groups all start on 16-byte boundaries); padding blocks hold zeros.
+template <int LPR>
+__device__ __forceinline__ double spmv4_rows(const BsrView<float>& A, const float* __restrict__ x,
+                                             float* __restrict__ y, bool want_dot) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / LPR, sl = lane % LPR;
+    constexpr int RPW = 32 / LPR;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
+        const int64_t row = base + sub;
+        const bool valid = row < A.n;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        if (valid) {
+            const int64_t rs = __ldg(A.indptr + row);
+            const int Lp = __ldg(A.indptr + row + 1) - int(rs);
+            const float* v0 = A.vals + 9 * rs;
+            for (int s = 4 * sl; s < Lp; s += 4 * LPR) {
+                const int4 c = __ldg(reinterpret_cast<const int4*>(A.indices + rs + s));
+                float4 w[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) w[q] = __ldg(reinterpret_cast<const float4*>(v0 + int64_t(q) * Lp + s));
+                const int cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    // component j of each value's float4 = slot s + j
+                    auto wq = [&](int q) { return j == 0 ? w[q].x : j == 1 ? w[q].y : j == 2 ? w[q].z : w[q].w; };
+                    const float* xc = x + 3 * int64_t(cc[j]);
+                    const float x0 = xc[0], x1 = xc[1], x2 = xc[2];
+                    a0 += wq(0) * x0 + wq(1) * x1 + wq(2) * x2;
+                    a1 += wq(3) * x0 + wq(4) * x1 + wq(5) * x2;
+                    a2 += wq(6) * x0 + wq(7) * x1 + wq(8) * x2;
+                }
+            }
+        }
+        a0 = group_sum<LPR>(a0);
+        a1 = group_sum<LPR>(a1);
+        a2 = group_sum<LPR>(a2);
+        if (valid && sl == 0) {
+            y[3 * row] = a0;
+            y[3 * row + 1] = a1;
+            y[3 * row + 2] = a2;
+            if (want_dot)
+                dot += double(x[3 * row]) * double(a0) + double(x[3 * row + 1]) * double(a1) +
+                       double(x[3 * row + 2]) * double(a2);
+        }
+    }
+    return dot;
+}
+
 // One pass of y = A x over the rows assigned to this thread; returns sum_rows x_i . y_i
 // for this lane's RHS (valid in the lane that writes the row), for PCG's p.q.
 template <typename T, int LPR>
 __device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
                                              bool want_dot) {
+    if constexpr (sizeof(T) == 4) {
+        if (A.rsoa == 2) return spmv4_rows<(LPR > 8 ? 8 : LPR)>(A, x, y, want_dot);
+    }
     const int lane = threadIdx.x & 31;
     const int sub = lane / LPR, sl = lane % LPR;
     constexpr int RPW = 32 / LPR;

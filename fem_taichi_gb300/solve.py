@@ -64,13 +64,22 @@ class DeviceSystem:
         return _stream(self.device)
 
     def K32(self):
-        """FP32 copy of K in the row-SoA layout (coalesced SpMV loads)."""
+        """FP32 copy of K in the padded row-SoA layout (rows rounded up to 4 blocks, so the
+        SpMV reads 4 slots of a value with one 16-byte load)."""
         if self._K32 is None:
-            self._K32 = torch.empty(9 * self.nnzb, dtype=torch.float32, device=self.device)
-            _lib.check(self.lib.fem_bsr_to_rsoa_f32(ctypes.byref(self.A64), _dptr(self._K32), self.stream),
-                       "fem_bsr_to_rsoa_f32")
-            self._A32 = FemBsr(self.n, self.nnzb, self.model.mesh.indptr.data_ptr(),
-                               self.model.mesh.indices.data_ptr(), self._K32.data_ptr(), FEM_F32, _lib.LAYOUT_RSOA)
+            P = self.model.Physics
+            ind = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+            ind4 = np.zeros(self.n + 1, dtype=np.int32)
+            _lib.check(self.lib.fem_rsoa4_indptr(self.n, ind.ctypes.data, ind4.ctypes.data), "fem_rsoa4_indptr")
+            nnzb4 = int(ind4[-1])
+            self._indptr4 = torch.from_numpy(ind4).to(self.device)
+            self._indices4 = torch.empty(max(nnzb4, 4), dtype=torch.int32, device=self.device)
+            self._K32 = torch.empty(9 * max(nnzb4, 4), dtype=torch.float32, device=self.device)
+            _lib.check(self.lib.fem_bsr_to_rsoa4_f32(ctypes.byref(self.A64), _dptr(self._indptr4),
+                                                     _dptr(self._indices4), _dptr(self._K32), self.stream),
+                       "fem_bsr_to_rsoa4_f32")
+            self._A32 = FemBsr(self.n, nnzb4, self._indptr4.data_ptr(), self._indices4.data_ptr(),
+                               self._K32.data_ptr(), FEM_F32, _lib.LAYOUT_RSOA4)
         return self._K32
 
     def block_jacobi(self) -> torch.Tensor:

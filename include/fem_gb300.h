@@ -184,6 +184,9 @@ int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat, const doub
 
 #define FEM_LAYOUT_RSOA 2 /* values of block row i stored [9][L_i] from 9*indptr[i] (value q of slot l
                              at 9*indptr[i] + q*L_i + l): lanes of a row read consecutive words */
+#define FEM_LAYOUT_RSOA4 3 /* FP32 row-SoA with every row padded to a multiple of 4 blocks (its own
+                              indptr/indices; padding blocks: column = the row, values 0), so a lane
+                              reads 4 slots of one value with one 16-byte load */
 
 typedef struct fem_bsr {
     int64_t n_brow, nnzb;   /* block rows (= nodes), 3x3 blocks                         */
@@ -191,7 +194,7 @@ typedef struct fem_bsr {
     const int32_t* indices; /* [nnzb]                                                   */
     const void* vals;       /* 9*nnzb values, double (FEM_F64) or float (FEM_F32)       */
     int dtype;
-    int layout;             /* FEM_LAYOUT_BSR ([nnzb][3][3]) or FEM_LAYOUT_RSOA         */
+    int layout;             /* FEM_LAYOUT_BSR ([nnzb][3][3]), _RSOA or _RSOA4 (FP32)    */
 } fem_bsr;
 
 /* y = A x (SOLVE_static.py:36, KL * U).  nrhs in {1,2,4,8,16,32}; x, y: [n_brow][3][nrhs]
@@ -203,8 +206,14 @@ int fem_spmv_autotune(const fem_bsr* A, int nrhs, const void* x, void* y, int re
                       float* best_ms, void* stream);
 /* dst[i] = (float)src[i]: the FP32 copy of K / of preconditioner blocks for the mixed solve. */
 int fem_convert_f64_to_f32(const double* src, float* dst, int64_t n, void* stream);
-/* FP32 row-SoA copy (FEM_LAYOUT_RSOA) of an FP64 BSR matrix: the inner-solve operator. */
+/* FP32 row-SoA copy (FEM_LAYOUT_RSOA) of an FP64 BSR matrix. */
 int fem_bsr_to_rsoa_f32(const fem_bsr* A, float* dst, void* stream);
+/* Padded FP32 row-SoA copy (FEM_LAYOUT_RSOA4), the inner-solve operator.  fem_rsoa4_indptr
+ * (HOST arrays) gives its row pointers indptr4[n_brow+1] (rows rounded up to multiples of 4
+ * blocks; nnzb4 = indptr4[n_brow]); fem_bsr_to_rsoa4_f32 fills indices4[nnzb4] and
+ * vals4[9*nnzb4] from the FP64 BSR matrix A (indptr4 on the device). */
+int fem_rsoa4_indptr(int64_t n_brow, const int32_t* indptr, int32_t* indptr4);
+int fem_bsr_to_rsoa4_f32(const fem_bsr* A, const int32_t* indptr4, int32_t* indices4, float* vals4, void* stream);
 /* Inverses of the 3x3 diagonal blocks (block-Jacobi preconditioner), FP64 and/or FP32
  * outputs [n_brow][9] (either may be NULL); *n_bad (device int) counts rows whose diagonal
  * block is missing or singular (identity used). */

@@ -130,3 +130,13 @@ def test_pipeline_plan_rejects_bad_parts():
     P = F.hex_block(2, 2, 2)
     with pytest.raises(_lib.FemError):
         _plan(P, 0)
+
+
+def test_rsoa4_row_pointers():
+    """Padded row-SoA row pointers: every row rounded up to a multiple of 4 blocks."""
+    P = F.hex_block(5, 4, 3, jitter=0.1, seed=1)
+    ind = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+    ind4 = np.zeros_like(ind)
+    _lib.check(_lib.load().fem_rsoa4_indptr(P.Num_Node, ind.ctypes.data, ind4.ctypes.data))
+    L = np.diff(ind)
+    assert np.array_equal(np.diff(ind4), (L + 3) // 4 * 4) and ind4[0] == 0
