@@ -18,7 +18,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "spmv.cuh"
+#include "pcg.cuh"
 
 namespace fem {
 
@@ -26,94 +26,7 @@ int bsr_spmv_any(const fem_bsr* A, int nrhs, const void* x, void* y, int variant
 
 namespace {
 
-constexpr int kMaxR = 32;
-constexpr int kThreads = 256;
-constexpr int kMaxCtas = 4096;
-constexpr int kSlots = 3;
-
-struct PcgState {
-    double rz[kMaxR], pq[kMaxR], alpha[kMaxR], beta[kMaxR], bb[kMaxR], rr[kMaxR], tol2[kMaxR];
-    double norm2[kMaxR];
-    int active[kMaxR];
-    int iters[kMaxR];
-    int it, done, status, maxit;
-    unsigned ticket;
-};
-
-// Sum of v over the lanes of this warp that hold the same right-hand side (lane % R).
-template <int R>
-__device__ __forceinline__ double warp_rhs_sum(double v) {
-#pragma unroll
-    for (int off = 16; off >= R; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
-
-// Block-level reduction of up to kSlots values per RHS into part[blockIdx.x]; returns true
-// in every thread of the CTA that finished last (after which part[] is complete).
-template <int R, int NS>
-__device__ bool block_partials(const double (&v)[NS], double* part, unsigned* ticket) {
-    __shared__ double sm[kThreads / 32][NS][kMaxR];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const double w = warp_rhs_sum<R>(v[s]);
-        if (lane < R) sm[warp][s][lane] = w;
-    }
-    __syncthreads();
-    if (threadIdx.x < R) {
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            double acc = 0.0;
-            for (int w = 0; w < int(blockDim.x / 32); ++w) acc += sm[w][s][threadIdx.x];
-            part[(int64_t(blockIdx.x) * kSlots + s) * kMaxR + threadIdx.x] = acc;
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (last) __threadfence();
-    return last;
-}
-
-// In the last CTA (all threads call it): tot[s][k] = sum over CTAs of slot s, RHS k.  The
-// kThreads / R threads of each RHS stride over the CTAs, then a fixed-shape tree in shared
-// memory combines them, so the result does not depend on timing.
-template <int R, int NS>
-__device__ void last_block_totals(const double* part, int nblocks, double (&tot)[NS][kMaxR]) {
-    constexpr int G = kThreads / R;
-    __shared__ double red[NS][kThreads];
-    const int t = threadIdx.x, k = t % R, g = t / R;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        double acc = 0.0;
-        for (int b = g; b < nblocks; b += G) acc += __ldcg(part + (int64_t(b) * kSlots + s) * kMaxR + k);
-        red[s][t] = acc;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int off = G / 2; off >= 1; off >>= 1) {
-        if (g < off) {
-#pragma unroll
-            for (int s = 0; s < NS; ++s) red[s][t] += red[s][t + off * R];
-        }
-        __syncthreads();
-    }
-    if (t < R) {
-#pragma unroll
-        for (int s = 0; s < NS; ++s) tot[s][t] = red[s][t];
-    }
-    __syncthreads();
-}
-
-// z = M r for one node / RHS, M the node's 3x3 preconditioner block.
-template <typename T>
-__device__ __forceinline__ void apply_block(const T* __restrict__ Mi, T r0, T r1, T r2, T& z0, T& z1, T& z2) {
-    z0 = Mi[0] * r0 + Mi[1] * r1 + Mi[2] * r2;
-    z1 = Mi[3] * r0 + Mi[4] * r1 + Mi[5] * r2;
-    z2 = Mi[6] * r0 + Mi[7] * r1 + Mi[8] * r2;
-}
+using namespace pcgd;
 
 // x = 0, r = b, z = M r; rz, rr -> state (bb = rr, tol2 = rtol^2 bb).
 template <typename T, int R>
@@ -121,6 +34,7 @@ __global__ void __launch_bounds__(kThreads) k_init(int64_t n, const T* __restric
                                                     T* x, T* r, T* z, double* part, PcgState* st, double rtol,
                                                     int maxit) {
     double v[2] = {0.0, 0.0};
+    Dot<T> d_rz, d_rr;
     const int64_t total_t = n * R;
     for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < ((total_t + 31) / 32) * 32;
          t += int64_t(gridDim.x) * blockDim.x) {
@@ -140,10 +54,16 @@ __global__ void __launch_bounds__(kThreads) k_init(int64_t n, const T* __restric
             z[o] = z0;
             z[o + R] = z1;
             z[o + 2 * R] = z2;
-            v[0] += double(r0) * double(z0) + double(r1) * double(z1) + double(r2) * double(z2);
-            v[1] += double(r0) * double(r0) + double(r1) * double(r1) + double(r2) * double(r2);
+            d_rz.add(r0, z0);
+            d_rz.add(r1, z1);
+            d_rz.add(r2, z2);
+            d_rr.add(r0, r0);
+            d_rr.add(r1, r1);
+            d_rr.add(r2, r2);
         }
     }
+    v[0] = d_rz.value();
+    v[1] = d_rr.value();
     if (!block_partials<R, 2>(v, part, &st->ticket)) return;
     __shared__ double tot[2][kMaxR];
     last_block_totals<R, 2>(part, gridDim.x, tot);
@@ -187,7 +107,9 @@ __global__ void __launch_bounds__(kThreads) k_p_update(int64_t nv, const T* __re
     }
 }
 
-// q = A p and p.q -> alpha = rz / pq on the device.
+// q = A p and p.q -> alpha = rz / pq on the device.  (Folding p = z + beta p into this
+// kernel as q = A z + beta q was measured slower: the row epilogue's extra loads sit on the
+// product's critical path, and the recurrence drifts from A p in FP32.)
 template <typename T, int LPR_OR_R>
 __global__ void __launch_bounds__(kThreads) k_spmv_pq(const BsrView<T> A, const T* __restrict__ p, T* __restrict__ q,
                                                        double* part, PcgState* st, int R) {
@@ -236,6 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_update(int64_t n, const T* __restr
                                                       PcgState* st) {
     if (st->done) return;
     double v[2] = {0.0, 0.0};
+    Dot<T> d_rz, d_rr;
     const int64_t total_t = n * R;
     for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < ((total_t + 31) / 32) * 32;
          t += int64_t(gridDim.x) * blockDim.x) {
@@ -256,10 +179,16 @@ __global__ void __launch_bounds__(kThreads) k_update(int64_t n, const T* __restr
             z[o] = z0;
             z[o + R] = z1;
             z[o + 2 * R] = z2;
-            v[0] += double(r0) * double(z0) + double(r1) * double(z1) + double(r2) * double(z2);
-            v[1] += double(r0) * double(r0) + double(r1) * double(r1) + double(r2) * double(r2);
+            d_rz.add(r0, z0);
+            d_rz.add(r1, z1);
+            d_rz.add(r2, z2);
+            d_rr.add(r0, r0);
+            d_rr.add(r1, r1);
+            d_rr.add(r2, r2);
         }
     }
+    v[0] = d_rz.value();
+    v[1] = d_rr.value();
     if (block_partials<R, 2>(v, part, &st->ticket)) {
         __shared__ double tot[2][kMaxR];
         last_block_totals<R, 2>(part, gridDim.x, tot);

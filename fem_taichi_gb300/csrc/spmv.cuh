@@ -23,6 +23,32 @@ struct BsrView {
     int rsoa;               // 1: row-SoA value layout; 2: row-SoA padded to 4-block multiples (FP32)
 };
 
+// Dot-product accumulator of the solver.  FP64 vectors: plain FP64 fused multiply-adds.
+// FP32 vectors: every product is formed exactly (FMA error term) and summed with a
+// compensated two-sum in FP32 pairs (about 48 significant bits), and becomes a double once
+// per thread, so the per-element work stays on the FP32 pipes (GB300's FP64 pipe is ~64x
+// slower) while the dot products keep FP64-class accuracy.
+template <typename T>
+struct Dot {
+    double v = 0.0;
+    __device__ __forceinline__ void add(T a, T b) { v = fma(double(a), double(b), v); }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <>
+struct Dot<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float a, float b) {
+        const float pr = __fmul_rn(a, b);
+        const float e = __fmaf_rn(a, b, -pr);
+        const float t = __fadd_rn(s, pr);
+        const float bb = __fsub_rn(t, s);
+        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(pr, bb));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(err, e));
+    }
+    __device__ __forceinline__ double value() const { return double(s) + double(c); }
+};
+
 // BsrView::rsoa for a fem_bsr layout code
 inline int rsoa_kind(int layout) {
     return layout == FEM_LAYOUT_RSOA ? 1 : layout == FEM_LAYOUT_RSOA4 ? 2 : 0;
@@ -42,18 +68,39 @@ __device__ __forceinline__ V group_sum(V v) {
     return v;
 }
 
+// Row epilogues.  The product kernels hand each finished row (and right-hand side k) to
+// an epilogue: o is the index of the row's first component in the [n][3][R] vectors,
+// `stride` = R, (a0, a1, a2) = (A x) of the row.
+
+// y = A x, and dot += x_row . y_row when asked (PCG's p.q).
+template <typename T>
+struct StoreY {
+    const T* x;
+    T* y;
+    bool want_dot;
+    __device__ __forceinline__ void operator()(int64_t o, int stride, int, T a0, T a1, T a2, Dot<T>& dot) const {
+        y[o] = a0;
+        y[o + stride] = a1;
+        y[o + 2 * stride] = a2;
+        if (want_dot) {
+            dot.add(x[o], a0);
+            dot.add(x[o + stride], a1);
+            dot.add(x[o + 2 * stride], a2);
+        }
+    }
+};
+
 // Padded row-SoA FP32 product: each lane takes 4 consecutive slots of its row per step and
 // reads each of the 9 values of those 4 blocks with one 16-byte load (rows, values and
 // slot groups all start on 16-byte boundaries); padding blocks hold zeros.
-template <int LPR>
-__device__ __forceinline__ double spmv4_rows(const BsrView<float>& A, const float* __restrict__ x,
-                                             float* __restrict__ y, bool want_dot) {
+template <int LPR, typename Epi>
+__device__ __forceinline__ double spmv4_rows_epi(const BsrView<float>& A, const float* __restrict__ x, const Epi& epi) {
     const int lane = threadIdx.x & 31;
     const int sub = lane / LPR, sl = lane % LPR;
     constexpr int RPW = 32 / LPR;
     const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
-    double dot = 0.0;
+    Dot<float> dot;
     for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
         const int64_t row = base + sub;
         const bool valid = row < A.n;
@@ -83,32 +130,24 @@ __device__ __forceinline__ double spmv4_rows(const BsrView<float>& A, const floa
         a0 = group_sum<LPR>(a0);
         a1 = group_sum<LPR>(a1);
         a2 = group_sum<LPR>(a2);
-        if (valid && sl == 0) {
-            y[3 * row] = a0;
-            y[3 * row + 1] = a1;
-            y[3 * row + 2] = a2;
-            if (want_dot)
-                dot += double(x[3 * row]) * double(a0) + double(x[3 * row + 1]) * double(a1) +
-                       double(x[3 * row + 2]) * double(a2);
-        }
+        if (valid && sl == 0) epi(3 * row, 1, 0, a0, a1, a2, dot);
     }
-    return dot;
+    return dot.value();
 }
 
-// One pass of y = A x over the rows assigned to this thread; returns sum_rows x_i . y_i
-// for this lane's RHS (valid in the lane that writes the row), for PCG's p.q.
-template <typename T, int LPR>
-__device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
-                                             bool want_dot) {
+// One pass of A x over the rows assigned to this thread (LPR lanes per block row; one RHS);
+// returns this lane's share of the epilogue's dot product.
+template <typename T, int LPR, typename Epi>
+__device__ __forceinline__ double spmv1_rows_epi(const BsrView<T>& A, const T* __restrict__ x, const Epi& epi) {
     if constexpr (sizeof(T) == 4) {
-        if (A.rsoa == 2) return spmv4_rows<(LPR > 8 ? 8 : LPR)>(A, x, y, want_dot);
+        if (A.rsoa == 2) return spmv4_rows_epi<(LPR > 8 ? 8 : LPR)>(A, x, epi);
     }
     const int lane = threadIdx.x & 31;
     const int sub = lane / LPR, sl = lane % LPR;
     constexpr int RPW = 32 / LPR;
     const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
-    double dot = 0.0;
+    Dot<T> dot;
     for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
         const int64_t row = base + sub;
         const bool valid = row < A.n;
@@ -129,27 +168,21 @@ __device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __res
         a0 = group_sum<LPR>(a0);
         a1 = group_sum<LPR>(a1);
         a2 = group_sum<LPR>(a2);
-        if (valid && sl == 0) {
-            y[3 * row] = a0;
-            y[3 * row + 1] = a1;
-            y[3 * row + 2] = a2;
-            if (want_dot)
-                dot += double(x[3 * row]) * double(a0) + double(x[3 * row + 1]) * double(a1) +
-                       double(x[3 * row + 2]) * double(a2);
-        }
+        if (valid && sl == 0) epi(3 * row, 1, 0, a0, a1, a2, dot);
     }
-    return dot;
+    return dot.value();
 }
 
-template <typename T, int R>
-__device__ __forceinline__ double spmm_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
-                                            bool want_dot) {
+// Many right-hand sides: lane = RHS (32 / R rows per warp), each block's values loaded once
+// per row group and applied to every RHS.
+template <typename T, int R, typename Epi>
+__device__ __forceinline__ double spmm_rows_epi(const BsrView<T>& A, const T* __restrict__ x, const Epi& epi) {
     const int lane = threadIdx.x & 31;
     const int sub = lane / R, rhs = lane % R;
     constexpr int RPW = 32 / R;
     const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
-    double dot = 0.0;
+    Dot<T> dot;
     for (int64_t base = warp * RPW; base < A.n; base += nwarps * RPW) {
         const int64_t row = base + sub;
         if (row >= A.n) continue;
@@ -166,16 +199,22 @@ __device__ __forceinline__ double spmm_rows(const BsrView<T>& A, const T* __rest
             a1 += __ldg(v + 3 * vs) * x0 + __ldg(v + 4 * vs) * x1 + __ldg(v + 5 * vs) * x2;
             a2 += __ldg(v + 6 * vs) * x0 + __ldg(v + 7 * vs) * x1 + __ldg(v + 8 * vs) * x2;
         }
-        T* yr = y + 3 * row * R + rhs;
-        yr[0] = a0;
-        yr[R] = a1;
-        yr[2 * R] = a2;
-        if (want_dot) {
-            const T* xr = x + 3 * row * R + rhs;
-            dot += double(xr[0]) * double(a0) + double(xr[R]) * double(a1) + double(xr[2 * R]) * double(a2);
-        }
+        epi(3 * row * R + rhs, R, rhs, a0, a1, a2, dot);
     }
-    return dot;
+    return dot.value();
+}
+
+// y = A x forms of the three products (dot: sum_rows x_i . y_i when want_dot).
+template <typename T, int LPR>
+__device__ __forceinline__ double spmv1_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
+                                             bool want_dot) {
+    return spmv1_rows_epi<T, LPR>(A, x, StoreY<T>{x, y, want_dot});
+}
+
+template <typename T, int R>
+__device__ __forceinline__ double spmm_rows(const BsrView<T>& A, const T* __restrict__ x, T* __restrict__ y,
+                                            bool want_dot) {
+    return spmm_rows_epi<T, R>(A, x, StoreY<T>{x, y, want_dot});
 }
 
 // SpMV launch variants picked by the autotuner (nrhs == 1): lanes per block row and CTA size.
