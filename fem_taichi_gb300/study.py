@@ -213,3 +213,21 @@ def c5_study(net, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3
     rows = compare(S, Ur, variants, F=Fm)
     return {"workload": f"c5 twisted slab 1200x120x15, 2,325,136 nodes, {nrhs} RHS", "reference": ref,
             "solves": rows}
+
+
+def solve_probe(cfg="c3", iterations=40, device="cuda"):
+    """A short, eager (no CUDA graph) run of the solver kernels for launch-list profiling:
+    autotunes both SpMV precisions, then runs `iterations` FP64 PCG iterations and
+    `iterations` FP32 inner iterations in one refinement step."""
+    P = _mesh.config_mesh(cfg)
+    extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
+    S = DeviceSystem(Model(cfg, P, STEEL, device=device, extra_loads=extra))
+    S.variant(False, 1)
+    S.variant(True, 1)
+    out = []
+    for mixed in (False, True):
+        _, st = S.solve(rtol=1e-10, mixed=mixed, maxit=iterations, inner_maxit=iterations, max_outer=1,
+                        use_graph=False, unroll=8)
+        out.append(st)
+    torch.cuda.synchronize()
+    return out
