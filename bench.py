@@ -388,6 +388,23 @@ def main():
                           "frac_hbm": sbytes / (sms * 1e-3) / 1e9 / peak, "Mnodes_per_s": N / sms / 1e3}
         line["stress"]["gpu_launches"] = 2 * ns
         line["host_setup_s"] = {"mesh_and_pattern": t_mesh}
+        # topology (incidence + block pattern + gather map): host C++ build vs device build
+        from fem_taichi_gb300 import mesh as M_
+        t0 = time.perf_counter()
+        ind, _ = M_.build_pattern(P.conn, N)
+        nep, nel, _ = M_.build_incidence(P.conn, N)
+        M_.build_gather_map(P.conn, ind, P.ReNode, nep, nel, N)
+        t_host = time.perf_counter() - t0
+        M_.build_topology_gpu(P.conn, N, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            M_.build_topology_gpu(P.conn, N, device=dev)
+        torch.cuda.synchronize()
+        t_gpu = (time.perf_counter() - t0) / 3
+        line["topology"] = {"host_threads": cpu_threads(), "host_s": t_host, "gpu_s": t_gpu,
+                            "note": "incidence + block pattern + gather map; gpu includes the conn upload and two "
+                                    "host syncs (nnzb read back)"}
 
     # -- static solve studies (seconds to 1e-8 relative error vs an FP64 reference) ---------------
     if not a.no_solve and rank == 0:

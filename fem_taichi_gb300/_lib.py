@@ -106,6 +106,11 @@ SIGNATURES = {
                                   c_size_t, c_void_p]),
     "fem_rsoa4_indptr": (c_int, [c_int64, c_void_p, c_void_p]),
     "fem_bsr_to_rsoa4_f32": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_topology_workspace_bytes": (c_size_t, [c_int64, c_int64]),
+    "fem_topology_count_gpu": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                       ctypes.POINTER(c_int64), c_void_p, c_size_t, c_void_p]),
+    "fem_topology_fill_gpu": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_size_t, c_void_p]),
     "fem_pipeline_plan": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                   c_void_p]),
     "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -80,10 +80,50 @@ def build_incidence(conn: np.ndarray, n_node: int):
     return ne_ptr, ne_list, co_elem
 
 
-class Physics:
-    """Reference ``Read`` duck type built from in-memory arrays."""
+def build_topology_gpu(conn, n_node: int, device="cuda"):
+    """Incidence, block pattern and gather map built on the device (fem_topology_*_gpu), the
+    same arrays as build_incidence + build_pattern + build_gather_map.  Returns a dict of
+    device int32 / uint8 tensors: ne_ptr, ne_list, co_elem, indptr, indices, ne_inv, slot_map."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("build_topology_gpu needs a CUDA device")
+    d = torch.device(device)
+    c = torch.as_tensor(np.ascontiguousarray(conn, dtype=np.int32)).to(d)
+    E = int(c.shape[0])
+    L = _lib.load()
+    st = ctypes.c_void_p(torch.cuda.current_stream(d).cuda_stream)
+    ws = torch.empty(max(int(L.fem_topology_workspace_bytes(n_node, E)), 16), dtype=torch.uint8, device=d)
+    t = {"ne_ptr": torch.empty(n_node + 1, dtype=torch.int32, device=d),
+         "ne_list": torch.empty(max(8 * E, 1), dtype=torch.int32, device=d),
+         "co_elem": torch.empty(max(n_node, 1), dtype=torch.int32, device=d),
+         "indptr": torch.empty(n_node + 1, dtype=torch.int32, device=d)}
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    nnzb = ctypes.c_int64(0)
+    _lib.check(L.fem_topology_count_gpu(n_node, E, p(c), p(t["ne_ptr"]), p(t["ne_list"]), p(t["co_elem"]),
+                                        p(t["indptr"]), ctypes.byref(nnzb), p(ws), ws.numel(), st),
+               "fem_topology_count_gpu")
+    t["indices"] = torch.empty(max(nnzb.value, 1), dtype=torch.int32, device=d)
+    t["ne_inv"] = torch.empty(max(8 * E, 1), dtype=torch.int32, device=d)
+    t["slot_map"] = torch.empty(max(64 * E, 1), dtype=torch.uint8, device=d)
+    _lib.check(L.fem_topology_fill_gpu(n_node, E, p(c), p(t["ne_ptr"]), p(t["ne_list"]), p(t["indptr"]),
+                                       p(t["indices"]), p(t["ne_inv"]), p(t["slot_map"]), p(ws), ws.numel(), st),
+               "fem_topology_fill_gpu")
+    t["indices"] = t["indices"][:nnzb.value]
+    t["ne_list"] = t["ne_list"][:8 * E]
+    t["ne_inv"] = t["ne_inv"][:8 * E]
+    t["slot_map"] = t["slot_map"][:64 * E]
+    t["co_elem"] = t["co_elem"][:n_node]
+    return t
 
-    def __init__(self, node_ids, xyz, elem_ids, Bounds=None, Forces=None, name="mesh"):
+
+class Physics:
+    """Reference ``Read`` duck type built from in-memory arrays.  topology='gpu' builds the
+    pattern, incidence and gather map on the device (same arrays, host copies kept)."""
+
+    def __init__(self, node_ids, xyz, elem_ids, Bounds=None, Forces=None, name="mesh", topology="host"):
+        if topology not in ("host", "gpu"):
+            raise ValueError("topology must be 'host' or 'gpu'")
+        self.topology = topology
         node_ids = np.asarray(node_ids, dtype=np.int64)
         xyz = np.asarray(xyz, dtype=np.float64)
         N = node_ids.size
@@ -104,11 +144,18 @@ class Physics:
         self.Nind = np.zeros((self.Num_MaxN,), dtype=np.int64)
         self.Nind[self.Node[0, :].astype(np.int64) - 1] = np.arange(self.Num_Node, dtype=np.int64)
         self.conn = np.ascontiguousarray(self.Nind[self.Elem[-8:]].T, dtype=np.int32)   # (E, 8)
-        self.SmNode, self.ReNode = build_pattern(self.conn, self.Num_Node)
+        if getattr(self, "topology", "host") == "gpu":
+            t = build_topology_gpu(self.conn, self.Num_Node)
+            h = {k: v.cpu().numpy() for k, v in t.items()}
+            self.SmNode, self.ReNode = h["indptr"], h["indices"]
+            self.ne_ptr, self.ne_list, self.CoElem = h["ne_ptr"], h["ne_list"], h["co_elem"]
+            self.ne_inv, self.slot_map = h["ne_inv"], h["slot_map"]
+        else:
+            self.SmNode, self.ReNode = build_pattern(self.conn, self.Num_Node)
+            self.ne_ptr, self.ne_list, self.CoElem = build_incidence(self.conn, self.Num_Node)
+            self.ne_inv, self.slot_map = build_gather_map(self.conn, self.SmNode, self.ReNode, self.ne_ptr,
+                                                          self.ne_list, self.Num_Node)
         self.CoNode = np.diff(self.SmNode)
-        self.ne_ptr, self.ne_list, self.CoElem = build_incidence(self.conn, self.Num_Node)
-        self.ne_inv, self.slot_map = build_gather_map(self.conn, self.SmNode, self.ReNode, self.ne_ptr,
-                                                      self.ne_list, self.Num_Node)
 
     @property
     def xyz(self) -> np.ndarray:

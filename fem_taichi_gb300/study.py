@@ -215,13 +215,19 @@ def c5_study(net, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3
             "solves": rows}
 
 
-def solve_probe(cfg="c3", iterations=40, device="cuda"):
+def solve_probe(cfg="c3", iterations=40, device="cuda", variant64=None, variant32=None):
     """A short, eager (no CUDA graph) run of the solver kernels for launch-list profiling:
-    autotunes both SpMV precisions, then runs `iterations` FP64 PCG iterations and
-    `iterations` FP32 inner iterations in one refinement step."""
+    picks both SpMV launch variants (autotuned unless given: under a profiler the tuner's
+    timings are distorted), then runs `iterations` FP64 PCG iterations and `iterations` FP32
+    inner iterations in one refinement step."""
     P = _mesh.config_mesh(cfg)
     extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
     S = DeviceSystem(Model(cfg, P, STEEL, device=device, extra_loads=extra))
+    if variant64 is not None:
+        S._variant[(False, 1)] = int(variant64)
+    if variant32 is not None:
+        S.K32()
+        S._variant[(True, 1)] = int(variant32)
     S.variant(False, 1)
     S.variant(True, 1)
     out = []

@@ -11,6 +11,7 @@
  *
  * Reference interfaces replaced (tianshao1992/FEM_taichi):
  *   fem_pattern_*          READ_physics.py:42-61       Read.pre_process (SmNode/ReNode/CoNode)
+ *   fem_topology_*_gpu     READ_physics.py:42-61       the same, built on the device
  *   fem_incidence_build    READ_physics.py:51-60       Elem_Node incidence, CoElem
  *   fem_assemble           FEM_model_csr.py:150-242    InstallIndexK, InstallMatrixK, InstallMatrixM,
  *                          FEM_model_bsr.py:163-259    InstallIndexM, InstallVectorF, LoadF, ModifyK,
@@ -70,6 +71,23 @@ int fem_incidence_build(int64_t n_node, int64_t n_elem, const int32_t* conn, int
 int fem_gather_map(int64_t n_node, int64_t n_elem, const int32_t* conn, const int32_t* indptr,
                    const int32_t* indices, const int32_t* ne_ptr, const int32_t* ne_list, int32_t* ne_inv,
                    uint8_t* slot_map);
+
+/* ---- topology on the device (DEVICE pointers) ----------------------------------- */
+/* Device build of the same arrays as fem_incidence_build + fem_pattern_count/fill +
+ * fem_gather_map (READ_physics.py:42-61, FEM_model_bsr.py:171-175), bit for bit.  Two calls
+ * with the same workspace (fem_topology_workspace_bytes, left unchanged between them):
+ *   fem_topology_count_gpu: ne_ptr [N+1], ne_list [8E], co_elem [N] (may be NULL),
+ *     indptr [N+1]; returns nnzb in *nnzb (HOST; the call synchronises the stream);
+ *   fem_topology_fill_gpu: indices [nnzb] and, if both are non-NULL, ne_inv [8E] and
+ *     slot_map [8E][8].
+ * Limits: at most 128 elements per node; otherwise FEM_ERR_INVALID (use the host build). */
+size_t fem_topology_workspace_bytes(int64_t n_node, int64_t n_elem);
+int fem_topology_count_gpu(int64_t n_node, int64_t n_elem, const int32_t* conn, int32_t* ne_ptr, int32_t* ne_list,
+                           int32_t* co_elem, int32_t* indptr, int64_t* nnzb, void* workspace,
+                           size_t workspace_bytes, void* stream);
+int fem_topology_fill_gpu(int64_t n_node, int64_t n_elem, const int32_t* conn, const int32_t* ne_ptr,
+                          const int32_t* ne_list, const int32_t* indptr, int32_t* indices, int32_t* ne_inv,
+                          uint8_t* slot_map, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- device mesh descriptor ---------------------------------------------------- */
 typedef struct fem_mesh {
