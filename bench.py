@@ -425,6 +425,7 @@ def main():
         if a.c5:
             r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=3000)
             sol["c5"] = brief(r5)
+        sol["modal_c1"] = study.modal_study("c1", num_eigen=100, num_block=10, device=dev)
         line["solve"] = sol
 
     # -- CPU baseline (rank 0, N = 1) -----------------------------------------------------------

@@ -173,10 +173,57 @@ __device__ __forceinline__ double spmv1_rows_epi(const BsrView<T>& A, const T* _
     return dot.value();
 }
 
+// Many right-hand sides on the padded row-SoA FP32 copy: one block row per warp, lane =
+// (slot group g, right-hand side k) with 32 / R slot groups; each lane takes 4 consecutive
+// slots per step (one 16-byte load per value, the same address for the R lanes of a group),
+// then the groups' partial sums are combined by xor-shuffles.
+template <int R, typename Epi>
+__device__ __forceinline__ double spmm4_rows_epi(const BsrView<float>& A, const float* __restrict__ x, const Epi& epi) {
+    constexpr int G = 32 / R;
+    const int lane = threadIdx.x & 31;
+    const int g = lane / R, rhs = lane % R;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    Dot<float> dot;
+    for (int64_t row = warp; row < A.n; row += nwarps) {
+        const int64_t rs = __ldg(A.indptr + row);
+        const int Lp = __ldg(A.indptr + row + 1) - int(rs);
+        const float* v0 = A.vals + 9 * rs;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int s = 4 * g; s < Lp; s += 4 * G) {
+            const int4 c = __ldg(reinterpret_cast<const int4*>(A.indices + rs + s));
+            float4 w[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) w[q] = __ldg(reinterpret_cast<const float4*>(v0 + int64_t(q) * Lp + s));
+            const int cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                auto wq = [&](int q) { return j == 0 ? w[q].x : j == 1 ? w[q].y : j == 2 ? w[q].z : w[q].w; };
+                const float* xc = x + 3 * int64_t(cc[j]) * R + rhs;
+                const float x0 = xc[0], x1 = xc[R], x2 = xc[2 * R];
+                a0 += wq(0) * x0 + wq(1) * x1 + wq(2) * x2;
+                a1 += wq(3) * x0 + wq(4) * x1 + wq(5) * x2;
+                a2 += wq(6) * x0 + wq(7) * x1 + wq(8) * x2;
+            }
+        }
+#pragma unroll
+        for (int off = R; off < 32; off <<= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+        }
+        if (g == 0) epi(3 * row * R + rhs, R, rhs, a0, a1, a2, dot);
+    }
+    return dot.value();
+}
+
 // Many right-hand sides: lane = RHS (32 / R rows per warp), each block's values loaded once
 // per row group and applied to every RHS.
 template <typename T, int R, typename Epi>
 __device__ __forceinline__ double spmm_rows_epi(const BsrView<T>& A, const T* __restrict__ x, const Epi& epi) {
+    if constexpr (sizeof(T) == 4) {
+        if (A.rsoa == 2) return spmm4_rows_epi<R>(A, x, epi);
+    }
     const int lane = threadIdx.x & 31;
     const int sub = lane / R, rhs = lane % R;
     constexpr int RPW = 32 / R;

@@ -1,0 +1,128 @@
+"""GPU modal solve: drop-in for ``SOLVE_eigen.Eigen_solver`` (SOLVE_eigen.py:9-89).
+
+The reference runs a shift-invert block Lanczos for K x = lambda M x on the CPU: Pardiso
+factorises K once (SOLVE_eigen.py:30-32) and every step applies K^-1 M to a block of
+``num_block`` vectors, with two passes of full M-orthogonal reorthogonalisation, then the
+block-tridiagonal projection is diagonalised (lambda = 1 / eig(T)) and the frequencies are
+sqrt(lambda) / 2 pi.
+
+Here every vector lives in HBM: M is applied as a BSR SpMM (the scalar-per-block mass matrix
+expanded to diagonal 3x3 blocks), each K^-1 M u is one multi-right-hand-side PCG solve of the
+whole block (FP32 inner solves inside FP64 refinement, ``fem_pcg_solve`` with the block padded
+to the next supported count), and the reorthogonalisation products are FP64 GEMMs on the
+device.  Only the (2 num_eigen)^2 projection T is diagonalised on the host.
+
+``Eigen_solver(Model).Solve_cpu(num_eigen, num_block)`` keeps the reference's signature and
+returns (freq (num_eigen,), vectors (3N, num_eigen)); it runs the GPU path (there is no CPU
+path).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import FemBsr, FEM_F64
+from .model import _dptr
+from .solve import DeviceSystem, padded_nrhs
+
+
+class Eigen_solver:
+    """Drop-in for SOLVE_eigen.Eigen_solver (Qtype 0)."""
+
+    def __init__(self, Model, Qtype=0):
+        self.Qtype = Qtype
+        self.Model = Model
+        self.system = None
+        self.last_stats = None
+        self._Mb = None
+
+    def _system(self) -> DeviceSystem:
+        if self.system is None:
+            self.system = DeviceSystem(self.Model)
+        return self.system
+
+    def _mass_operator(self):
+        """M as FP64 BSR with diagonal 3x3 blocks m_ij I (same pattern as K)."""
+        if self._Mb is None:
+            S = self._system()
+            _, M, _ = self.Model.assemble(K=False, M=True, F=False, m_layout="bsr")
+            Mb = torch.zeros((S.nnzb, 3, 3), dtype=torch.float64, device=S.device)
+            for i in range(3):
+                Mb[:, i, i] = M
+            self._Mb = Mb
+            self._AM = FemBsr(S.n, S.nnzb, self.Model.mesh.indptr.data_ptr(), self.Model.mesh.indices.data_ptr(),
+                              Mb.data_ptr(), FEM_F64, _lib.LAYOUT_BSR)
+        return self._AM
+
+    def _apply_M(self, X: torch.Tensor) -> torch.Tensor:
+        """M X for an (n, b) block (b padded to a supported right-hand-side count; blocks wider
+        than 32 columns are applied 32 at a time)."""
+        if X.shape[1] > 32:
+            return torch.cat([self._apply_M(X[:, j:j + 32]) for j in range(0, X.shape[1], 32)], 1)
+        S = self._system()
+        A = self._mass_operator()
+        b = X.shape[1]
+        R = padded_nrhs(b)
+        Xp = X if R == b else torch.cat([X, X.new_zeros((X.shape[0], R - b))], 1)
+        Xp = Xp.contiguous()
+        Y = torch.empty_like(Xp)
+        _lib.check(S.lib.fem_bsr_spmv(ctypes.byref(A), R, _dptr(Xp), _dptr(Y), 0, S.stream), "fem_bsr_spmv (M)")
+        return Y[:, :b]
+
+    def Solve_gpu(self, num_eigen=100, num_block=10, rtol=1e-11, seed=0, u0=None, mixed=True):
+        """Block Lanczos (SOLVE_eigen.py:45-89) on the device.  Returns (lambda (num_eigen,),
+        vectors (3N, num_eigen)) as device tensors, lambda ascending."""
+        if self.Qtype != 0:
+            raise NotImplementedError("only the linear modal problem (Qtype 0) is built")
+        S = self._system()
+        n = 3 * S.n
+        b = int(num_block)
+        m = 2 * int(num_eigen)
+        steps = int(m / b)
+        if b < 1 or b > 32 or steps < 1:
+            raise ValueError("need 1 <= num_block <= 32 and 2*num_eigen >= num_block")
+        dev = S.device
+        if u0 is None:
+            u0 = np.random.default_rng(seed).uniform(size=(n, b))
+        u = torch.as_tensor(np.asarray(u0, dtype=np.float64), device=dev).reshape(n, b)
+        Q = torch.zeros((n, m), dtype=torch.float64, device=dev)
+        T = np.zeros((m, m))
+        v = torch.linalg.cholesky(u.T @ self._apply_M(u)).T         # upper, u^T M u = v^T v
+        u = torch.linalg.solve_triangular(v, u, upper=True, left=False)
+        Q[:, :b] = u
+        iters = 0
+        for i in range(steps):
+            w, st = S.solve(F=self._apply_M(u), rtol=rtol, mixed=mixed)
+            if st["status"] != 0:
+                raise _lib.FemError(st["status"], f"K solve of Lanczos step {i}: {st['status_text']}")
+            iters += st["iterations"]
+            w = w.reshape(n, b)
+            Tii = u.T @ self._apply_M(w)
+            T[i * b:(i + 1) * b, i * b:(i + 1) * b] = Tii.cpu().numpy()
+            w = w - u @ Tii
+            if i >= steps - 1:
+                break
+            Qi = Q[:, :(i + 1) * b]
+            for _ in range(2):
+                w = w - Qi @ (Qi.T @ self._apply_M(w))
+            t = torch.linalg.cholesky(w.T @ self._apply_M(w)).T
+            T[(i + 1) * b:(i + 2) * b, i * b:(i + 1) * b] = t.cpu().numpy()
+            T[i * b:(i + 1) * b, (i + 1) * b:(i + 2) * b] = t.T.cpu().numpy()
+            u = torch.linalg.solve_triangular(t, w, upper=True, left=False)
+            Q[:, (i + 1) * b:(i + 2) * b] = u
+        ev, vec = np.linalg.eigh(T)
+        lam = 1.0 / ev
+        order = np.argsort(lam)[:num_eigen]
+        X = Q @ torch.as_tensor(vec[:, order], device=dev)
+        self.last_stats = {"steps": steps, "solve_iterations": iters}
+        return torch.as_tensor(lam[order], device=dev), X
+
+    def Solve_cpu(self, num_eigen=100, num_block=10):
+        """SOLVE_eigen.py:14-43 signature: returns (freq (num_eigen,), vectors (3N, num_eigen))
+        as numpy arrays, freq = sqrt(lambda) / 2 pi (SOLVE_eigen.py:36)."""
+        lam, X = self.Solve_gpu(num_eigen=num_eigen, num_block=num_block)
+        freq = torch.sqrt(lam) / 2 / np.pi
+        return freq.cpu().numpy(), X.cpu().numpy()

@@ -148,6 +148,30 @@ def spmv_rates(S: DeviceSystem, reps=20, peak_gbs=None):
     return out
 
 
+def spmm_rates(S: DeviceSystem, nrhs_list=(2, 4, 8, 16, 32), reps=10, peak_gbs=None):
+    """CUDA-event time of the multi-right-hand-side products (FP64 BSR and the FP32 copy)."""
+    out = {}
+    stream = torch.cuda.current_stream(S.device)
+    for fp32, name, vb in ((False, "fp64", 8), (True, "fp32", 4)):
+        for R in nrhs_list:
+            x = torch.ones((3 * S.n, R), dtype=torch.float32 if fp32 else torch.float64, device=S.device)
+            for _ in range(2):
+                S.spmv(x, fp32=fp32, nrhs=R)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                S.spmv(x, fp32=fp32, nrhs=R)
+            e1.record(stream)
+            torch.cuda.synchronize(S.device)
+            ms = e0.elapsed_time(e1) / reps
+            b = spmv_bytes(S.n, S.nnzb, vb, R)
+            out[f"{name}_r{R}"] = {"ms": ms, "gbs": b / (ms * 1e-3) / 1e9, "ms_per_rhs": ms / R}
+            if peak_gbs:
+                out[f"{name}_r{R}"]["frac_hbm"] = out[f"{name}_r{R}"]["gbs"] / peak_gbs
+    return out
+
+
 def c3_study(device="cuda", rtol=1e-10, peak_gbs=None):
     P = _mesh.config_mesh("c3")
     extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
@@ -237,3 +261,24 @@ def solve_probe(cfg="c3", iterations=40, device="cuda", variant64=None, variant3
         out.append(st)
     torch.cuda.synchronize()
     return out
+
+
+def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda"):
+    """Block-Lanczos modal solve (SOLVE_eigen.py:45-89, the reference driver's num_eigen=100)
+    on a config mesh: wall time of a warm solve and the lowest frequencies."""
+    from .eigen import Eigen_solver
+    P = _mesh.config_mesh(cfg)
+    M = Model(cfg, P, STEEL, device=device)
+    solver = Eigen_solver(M)
+    solver.Solve_gpu(num_eigen=min(num_eigen, 10), num_block=min(num_block, 5))  # warm: FP32 copy, graphs
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    lam, X = solver.Solve_gpu(num_eigen=num_eigen, num_block=num_block)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t
+    freq = (torch.sqrt(lam) / 2 / np.pi).cpu().numpy()
+    G = X.T @ solver._apply_M(X)
+    orth = float((G - torch.eye(num_eigen, dtype=G.dtype, device=G.device)).abs().max())
+    return {"workload": f"{cfg}: {P.Num_Node:,} nodes, {num_eigen} modes, block {num_block}", "wall_s": wall,
+            "steps": solver.last_stats["steps"], "solve_iterations": solver.last_stats["solve_iterations"],
+            "lowest_freq_hz": [float(f) for f in freq[:5]], "M_orthonormality_err": orth}
