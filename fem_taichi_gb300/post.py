@@ -14,6 +14,7 @@ an out-of-range index of a 2-entry dense field onto its low bit would read.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 import torch
@@ -43,6 +44,35 @@ def extrapolation_table(gmat_mode: str = "written") -> np.ndarray:
                 0.125 * (1 + a) * (1 + b) * (1 + c), 0.125 * (1 - a) * (1 + b) * (1 + c),
                 0.125 * (1 - a) * (1 - b) * (1 + c), 0.125 * (1 + a) * (1 - b) * (1 + c)]
     return W
+
+
+def write_tecplot_ascii(output_file, title, Physics, Fields, Field_names):
+    """Tecplot ASCII FE-point file, as POST_process.py:101-135 (Output_field_ASC) writes it:
+    a TITLE line, the VARIABLES line (x, y, z, then every field name per step, numbered from 1),
+    the ZONE line (I = nodes, J = elements, FEPOINT, BRICK), one row per node (x y z and the
+    fields of every step, '%10.5e', space separated, NaN written empty) and one row per element
+    (its 8 nodes, 1-based).  Fields: (N, n_fields, n_steps)."""
+    Fields = np.asarray(Fields, dtype=np.float64)
+    Node = Physics.Node[-3:]
+    N = Node.shape[-1]
+    if Fields.ndim != 3 or Fields.shape[0] != N:
+        raise ValueError("Fields must be (N, n_fields, n_steps)")
+    data = np.concatenate((Node.T, Fields.transpose(0, 2, 1).reshape(N, -1)), axis=-1)
+    conn = Physics.Nind[np.asarray(Physics.Elem[-8:], dtype=np.int64)].T + 1
+    head = ['TITLE = "' + title + '.data"\n', 'VARIABLES = "X [ m ]","Y [ m ]","Z [m]"']
+    for step in range(Fields.shape[-1]):
+        for name in Field_names:
+            head.append(',"' + " " + str(name) + str(step + 1) + '"')  # ("%s " % ',"') + name + step + '"'
+    head.append("\n")
+    head.append("ZONE  I=" + str(N) + ", J=" + str(conn.shape[0]) + ", F=FEPOINT, ET=BRICK\n")
+    txt = np.char.mod("%10.5e", data)
+    txt[np.isnan(data)] = ""
+    with open(output_file, "w") as f:
+        f.write("".join(head))
+        f.write("\n".join(" ".join(r) for r in txt))
+        f.write("\n")
+        f.write("\n".join(" ".join(map(str, r)) for r in conn.tolist()))
+        f.write("\n")
 
 
 class Post:
@@ -86,3 +116,18 @@ class Post:
     def Get_Stress(self) -> np.ndarray:
         """POST_process.py:72-99."""
         return self.stress_device().cpu().numpy()
+
+    @property
+    def path(self) -> str:
+        """Results directory of the reference (POST_process.py:20, "Results/<name>/")."""
+        return os.path.join("Results", self.name) + os.sep
+
+    def Output_field_ASC(self, file_name, Fields, Field_names):
+        """POST_process.py:101-135: Tecplot ASCII file <path><file_name>.dat (the directory is
+        created on the first write instead of in the constructor)."""
+        os.makedirs(self.path, exist_ok=True)
+        write_tecplot_ascii(self.path + file_name + ".dat", self.name, self.Physics, Fields, Field_names)
+
+    def Output_field_BIN(self, file_name, Fields, Field_names):
+        """POST_process.py:32-69 writes through the Windows TecIO library; not available."""
+        raise NotImplementedError("binary Tecplot output needs the closed TecIO library; use Output_field_ASC")

@@ -140,3 +140,27 @@ def test_rsoa4_row_pointers():
     _lib.check(_lib.load().fem_rsoa4_indptr(P.Num_Node, ind.ctypes.data, ind4.ctypes.data))
     L = np.diff(ind)
     assert np.array_equal(np.diff(ind4), (L + 3) // 4 * 4) and ind4[0] == 0
+
+
+def test_tecplot_ascii_output(tmp_path):
+    """POST_process.py:101-135 layout: header lines, node rows (x y z + fields per step,
+    '%10.5e', NaN empty), element rows with 1-based node numbers."""
+    from fem_taichi_gb300.post import write_tecplot_ascii
+    P = F.hex_block(3, 2, 2, jitter=0.1, seed=1)
+    rng = np.random.default_rng(0)
+    Fld = rng.standard_normal((P.Num_Node, 4, 2))
+    Fld[1, 2, 0] = np.nan
+    out = tmp_path / "s.dat"
+    write_tecplot_ascii(str(out), "blk", P, Fld, ["u", "v", "w", "s"])
+    lines = out.read_text().splitlines()
+    assert lines[0] == 'TITLE = "blk.data"'
+    assert lines[1] == 'VARIABLES = "X [ m ]","Y [ m ]","Z [m]"' + "".join(
+        f'," {n}{s}"' for s in (1, 2) for n in "uvws")
+    assert lines[2] == f"ZONE  I={P.Num_Node}, J={P.Num_Elem}, F=FEPOINT, ET=BRICK"
+    rows = lines[3:3 + P.Num_Node]
+    assert rows[1].split(" ")[3 + 2] == ""            # NaN written empty
+    vals = np.array([float(x) for x in rows[0].split(" ")])
+    ref = np.concatenate([P.xyz[0], Fld[0].T.reshape(-1)])
+    assert np.allclose(vals, ref, rtol=1e-5)
+    conn = np.array([[int(x) for x in r.split(" ")] for r in lines[3 + P.Num_Node:]])
+    assert np.array_equal(conn, P.conn + 1)
