@@ -438,6 +438,36 @@ def main():
                                 "sample": f"{ns} assemblies (K+M+F) of the {S.grid[0]}x{S.grid[1]}x{S.grid[2]} "
                                           f"block of the {a.config} family ({S.Num_Elem:,} elements) with "
                                           f"oracle/fem_oracle.c on {thr} threads, {t:.2f} s each"}
+        if not a.no_extras:
+            # stress recovery: the C restatement on the same sample mesh, all host threads
+            from oracle import c_oracle as C
+            from oracle import fem_oracle as O
+            us = np.random.default_rng(2).uniform(-1e-3, 1e-3, size=(S.Num_Node, 3))
+            W = O.extrapolation_table("written")
+            C.stress(S.xyz, S.conn, S.CoElem, mat, us, W, nthreads=thr)
+            t0 = time.perf_counter()
+            C.stress(S.xyz, S.conn, S.CoElem, mat, us, W, nthreads=thr)
+            ts = time.perf_counter() - t0
+            line["cpu_baseline"]["stress"] = {"Mnodes_per_s": S.Num_Node / ts / 1e6, "s": ts, "cores": thr,
+                                              "sample": f"{S.Num_Node:,} nodes of the same sample mesh"}
+        if not a.no_solve:
+            # static solve: FP64 block-Jacobi PCG with scipy products (1 thread) on the c3
+            # system, a bounded sample of iterations scaled to the GPU FP64 solver's count
+            from oracle import solve_oracle as SO
+            P3 = F.config_mesh("c3")
+            M3 = F.Model("c3", P3, mat, extra_loads=F.face_traction_loads(P3, "zmax", (0.0, 0.0, -1.0)),
+                         device=dev)
+            K3, F3 = M3.Get_MatrixKL(), M3.Get_VectorF()
+            _, it, tsol = SO.bj_pcg(K3, F3, rtol=1e-10, maxit=30)
+            gpu_it = next(r["iterations"] for r in line.get("solve", {}).get("c3", {}).get("solves", [])
+                          if r["label"] == "fp64_bj") if "solve" in line else None
+            est = tsol / it * gpu_it if gpu_it else None
+            line["cpu_baseline"]["solve"] = {
+                "kind": "port", "cores": 1, "s_per_iteration": tsol / it,
+                "c3_fp64_bj_estimated_s": est,
+                "sample": f"{it} FP64 block-Jacobi PCG iterations on c3 (214,221 nodes) with scipy products, "
+                          f"scaled to the {gpu_it} iterations the same method takes to 1e-10; Pardiso "
+                          "(the reference's solver) is not available"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
