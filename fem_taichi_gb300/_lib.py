@@ -111,6 +111,9 @@ SIGNATURES = {
                                        ctypes.POINTER(c_int64), c_void_p, c_size_t, c_void_p]),
     "fem_topology_fill_gpu": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fem_tangent_workspace_bytes": (c_size_t, [c_int64]),
+    "fem_assemble_tangent": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), c_void_p, c_int, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "fem_pipeline_plan": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                   c_void_p]),
     "fem_csr_index": (c_int, [ctypes.POINTER(FemMesh), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

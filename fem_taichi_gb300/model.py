@@ -137,6 +137,7 @@ class Model:
         self._version = 0          # bumped whenever an assembly input changes
         self._cache = None         # (version, {"K", "M", "F"} host arrays not yet handed out)
         self._plan = None
+        self.U = None              # large-displacement state (LDinit)
         self.pipeline_parts = 8    # parts of fem_assemble_host (copies overlap the next part)
         if algo not in ("dd", "fp64"):
             raise ValueError("algo must be 'dd' or 'fp64'")
@@ -270,8 +271,33 @@ class Model:
         """FEM_model_csr.py:141-146: element centrifugal loads + nodal loads, node-major (3N,)."""
         return self._take("F")
 
-    def Get_MatrixKN(self):
-        raise NotImplementedError("large-displacement tangent (FEM_model_bsr.py:134-145) is not built")
-
+    # -- large displacement (FEM_model_bsr.py:134-145, 476-598) ----------------------------
     def LDinit(self, displace):
-        raise NotImplementedError("large-displacement tangent (FEM_model_bsr.py:595-598) is not built")
+        """FEM_model_bsr.py:595-598: set the nodal displacements (3N,) the tangent is taken at."""
+        self.U = torch.as_tensor(np.asarray(displace, dtype=np.float64).reshape(-1, 3)).to(self.device).contiguous()
+
+    def assemble_tangent(self, k_layout="bsr"):
+        """Device (KT, KM) at the displacements of LDinit: (nnzb, 3, 3) BSR or (9 nnzb,) CSR order."""
+        if getattr(self, "U", None) is None:
+            self.LDinit(np.zeros(self.Num_Free))
+        d = self.device
+        nnzb = self.mesh.nnzb
+        shape = (nnzb, 3, 3) if k_layout == "bsr" else (9 * nnzb,)
+        KT = torch.empty(shape, dtype=torch.float64, device=d)
+        KM = torch.empty(shape, dtype=torch.float64, device=d)
+        nbytes = max(int(self.lib.fem_tangent_workspace_bytes(self.Num_Elem)), 16)
+        if getattr(self, "_tws", None) is None or self._tws.numel() < nbytes:
+            self._tws = torch.empty(nbytes, dtype=torch.uint8, device=d)
+        _lib.check(self.lib.fem_assemble_tangent(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), _dptr(self.U),
+                                                 LAYOUT_BSR if k_layout == "bsr" else LAYOUT_CSR, _dptr(KT),
+                                                 _dptr(KM), _dptr(self.fixed), _dptr(self._tws),
+                                                 self._tws.numel(), _stream(d)), "fem_assemble_tangent")
+        return KT, KM
+
+    def Get_MatrixKN(self):
+        """FEM_model_bsr.py:134-145: (KT, KM) as scipy CSR at the displacements of LDinit."""
+        KT, KM = self.assemble_tangent(k_layout="csr")
+        rowK, colK, _, _ = self.csr_index()
+        n = self.Num_Free
+        mk = lambda V: sp.csr_matrix((V.cpu().numpy(), colK, rowK), shape=(n, n), dtype=np.float64)  # noqa: E731
+        return mk(KT), mk(KM)

@@ -180,12 +180,50 @@ class Static_solver:
             self.system = DeviceSystem(self.Model)
         return self.system
 
+    def Solve_nonlinear(self, max_errs=1e-4, max_iters=20, rtol=1e-10, mixed=True):
+        """Large-displacement Newton iteration of SOLVE_static.py:41-75 on the device.  Each
+        step: tangent KT and secant KM at U (Model.assemble_tangent), residual RF = KM U - F,
+        stop when ||RF|| / ||F|| <= max_errs or after max_iters steps, else KT dU = RF by PCG
+        and U -= dU.  (The reference solves KT dU = F at SOLVE_static.py:72, which does not
+        converge; this is the Newton-Raphson step that line stands for.)  Returns U (3N,) numpy;
+        self.last_stats["residuals"] holds the relative residual of every step."""
+        M = self.Model
+        dev = M.device
+        F = torch.as_tensor(M.Get_VectorF(), dtype=torch.float64).to(dev)
+        fn = float(torch.linalg.norm(F))
+        U = torch.zeros_like(F)
+        res, its = [], 0
+        step = 0
+        while True:
+            M.LDinit(U.cpu().numpy())
+            KT, KM = M.assemble_tangent(k_layout="bsr")
+            A = FemBsr(M.Num_Node, M.mesh.nnzb, M.mesh.indptr.data_ptr(), M.mesh.indices.data_ptr(),
+                       KM.data_ptr(), FEM_F64, _lib.LAYOUT_BSR)
+            KU = torch.empty_like(U)
+            _lib.check(M.lib.fem_bsr_spmv(ctypes.byref(A), 1, _dptr(U), _dptr(KU), 0,
+                                          ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), "KM U")
+            RF = KU - F
+            err = float(torch.linalg.norm(RF)) / fn if fn > 0 else 0.0
+            res.append(err)
+            if err <= max_errs or step == max_iters:
+                break
+            S = DeviceSystem(M, K=KT, F=RF)
+            dU, st = S.solve(F=RF, rtol=rtol, mixed=mixed)
+            if st["status"] != 0:
+                raise _lib.FemError(st["status"], f"Newton step {step}: {st['status_text']}")
+            its += st["iterations"]
+            U = U - dU
+            step += 1
+        self.last_stats = {"residuals": res, "steps": step, "pcg_iterations": its,
+                           "converged": res[-1] <= max_errs}
+        return U.cpu().numpy()
+
     def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, **kw):
         """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'learned' (uses
         ``self.Model.learned_precond`` (N, 9) if set, falling back to block Jacobi when the
         learned solve does not converge) or an (N, 9) array."""
         if self.Qtype != 0:
-            raise NotImplementedError("large-displacement Newton solve (SOLVE_static.py:41-75) is not built")
+            raise ValueError("Solve_gpu is the linear solve; Qtype=1 uses Solve_cpu / Solve_nonlinear")
         S = self._system()
         P = None
         fallback = False
@@ -208,6 +246,9 @@ class Static_solver:
         return U.cpu().numpy()
 
     def Solve_cpu(self, max_errs=1e-4, max_iters=20):
-        """SOLVE_static.py:12-39 signature (Qtype 0): returns U (3N,).  Runs the GPU solve
-        to a relative residual of 1e-12 (the reference used a direct factorisation)."""
+        """SOLVE_static.py:12-75 signature: returns U (3N,).  Qtype 0 runs the GPU linear solve
+        to a relative residual of 1e-12 (the reference used a direct factorisation); Qtype 1
+        the large-displacement Newton iteration (Solve_nonlinear)."""
+        if self.Qtype == 1:
+            return self.Solve_nonlinear(max_errs=max_errs, max_iters=max_iters)
         return self.Solve_gpu(rtol=1e-12, mixed=True)

@@ -17,6 +17,7 @@
  *                          FEM_model_bsr.py:163-259    InstallIndexM, InstallVectorF, LoadF, ModifyK,
  *                                                      UnitMatrixK/M, UnitVectorF, installLocalB/N
  *   fem_csr_index          FEM_model_csr.py:163,167-173,191,195-201   RowK/ColK/RowM/ColM
+ *   fem_assemble_tangent   FEM_model_bsr.py:134-145,178-191,476-592   Get_MatrixKN (large displacement)
  *   fem_stress             POST_process.py:172-209,72-99  get_NdSol, get_NdAve, UnitVectorS,
  *                                                      shapefunc_GS, Get_Stress (eigh, "VM")
  *   fem_bsr_spmv*          SOLVE_static.py:36          KL * U (residual product)
@@ -160,6 +161,17 @@ int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_a
 int fem_pipeline_plan(int64_t n_node, int64_t n_elem, const int32_t* indptr, const int32_t* ne_ptr,
                       const int32_t* ne_list, int n_parts, int64_t* row_split, int64_t* elem_split,
                       int64_t* block_split);
+
+/* Large-displacement tangent KT and secant KM at nodal displacements u ([n_node][3]):
+ * Get_MatrixKN / InstallMatrixKN / UnitK (FEM_model_bsr.py:134-145,178-191,476-592), with the
+ * penalty of ModifyMatrixK on both (:248-259).  FP64 element integrals, gathered like K
+ * (atomic-free, fixed order).  KT, KM: 9*nnzb values each in k_layout (BSR or the reference
+ * CSR order); fixed: per-node DOF bit mask as in fem_assembly_out, or NULL.  Needs
+ * mesh->ne_inv and mesh->slot_map. */
+size_t fem_tangent_workspace_bytes(int64_t n_elem);
+int fem_assemble_tangent(const fem_mesh* mesh, const fem_material* mat, const double* u, int k_layout,
+                         double* KT, double* KM, const uint8_t* fixed, void* workspace, size_t workspace_bytes,
+                         void* stream);
 
 /* Reference CSR index arrays (depend on the pattern only): rowK [3N+1], colK [9 nnzb],
  * rowM [3N+1], colM [3 nnzb]; any may be NULL. */

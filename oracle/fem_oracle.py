@@ -287,6 +287,83 @@ class OracleModel:
             F += (Jdet[:, None, None] * NR[g][None, :, None]) * f[:, None, :]
         return F
 
+    def element_KN(self, e0, e1, U):
+        """UnitK, FEM_model_bsr.py:476-515 (large displacement): tangent KT and secant KM blocks
+        of elements [e0, e1) at nodal displacements U (N, 3).
+
+        T = CoordU . DN is the displacement gradient; BN1/BN2 (InslocalBN, :544-592) its
+        nonlinear strain operators.  S accumulates D (B + BN/2) u_j over corners j and over
+        Gauss points in order without being reset between Gauss points (:491-494), and the
+        geometric term of Gauss point g uses the sum reached after g (MatrixS, :517-525;
+        :508-513).  KT += det (A + B), KM += det (A + B/2) with A = (B1+BN1)^T D0 B1 +
+        (B2+BN2)^T D1 B2 and B the same with BN in place of B on the right (:496-506)."""
+        C = self.coord[e0:e1]
+        n = C.shape[0]
+        Ue = np.asarray(U, dtype=np.float64)[self.nodes[e0:e1]]          # (n, 8, 3) corner u
+        CU = Ue.transpose(0, 2, 1)                                       # (n, 3, 8) CoordU
+        S0 = np.zeros((n, 3))
+        S1 = np.zeros((n, 3))
+        KT = np.zeros((n, 8, 8, 3, 3))
+        KM = np.zeros((n, 8, 8, 3, 3))
+        for g in range(8):
+            DNr = DNR[g]
+            J = C @ DNr
+            DN = DNr[None] @ inv3(J)                                     # (n, 8, 3)
+            Jdet = det3(J)
+            T = CU @ DN                                                  # (n, 3, 3)
+            B1 = np.zeros((n, 8, 3, 3))
+            B1[:, :, 0, 0], B1[:, :, 1, 1], B1[:, :, 2, 2] = DN[..., 0], DN[..., 1], DN[..., 2]
+            B2 = np.zeros((n, 8, 3, 3))
+            B2[:, :, 0, 1], B2[:, :, 0, 2] = DN[..., 2], DN[..., 1]
+            B2[:, :, 1, 0], B2[:, :, 1, 2] = DN[..., 2], DN[..., 0]
+            B2[:, :, 2, 0], B2[:, :, 2, 1] = DN[..., 1], DN[..., 0]
+            BN1 = np.zeros((n, 8, 3, 3))
+            BN2 = np.zeros((n, 8, 3, 3))
+            for m in range(3):                                           # BN1[m, k] = T[k, m] DN[j, m]
+                BN1[:, :, m, :] = T[:, None, :, m] * DN[:, :, m, None]
+            BN2[:, :, 0, :] = T[:, None, :, 2] * DN[:, :, 1, None] + T[:, None, :, 1] * DN[:, :, 2, None]
+            BN2[:, :, 1, :] = T[:, None, :, 2] * DN[:, :, 0, None] + T[:, None, :, 0] * DN[:, :, 2, None]
+            BN2[:, :, 2, :] = T[:, None, :, 1] * DN[:, :, 0, None] + T[:, None, :, 0] * DN[:, :, 1, None]
+            for j in range(8):
+                t1 = np.einsum('erp,ep->er', B1[:, j] + 0.5 * BN1[:, j], Ue[:, j])
+                t2 = np.einsum('erp,ep->er', B2[:, j] + 0.5 * BN2[:, j], Ue[:, j])
+                S0 += t1 @ self.D0.T
+                S1 += t2 @ self.D1.T
+            P1, P2 = B1 + BN1, B2 + BN2
+            A = (np.einsum('ejrp,rs,eksq->ejkpq', P1, self.D0, B1, optimize=True)
+                 + np.einsum('ejrp,rs,eksq->ejkpq', P2, self.D1, B2, optimize=True))
+            Bm = (np.einsum('ejrp,rs,eksq->ejkpq', P1, self.D0, BN1, optimize=True)
+                  + np.einsum('ejrp,rs,eksq->ejkpq', P2, self.D1, BN2, optimize=True))
+            w = Jdet[:, None, None, None, None]
+            KT += w * (A + Bm)
+            KM += w * (A + 0.5 * Bm)
+            s = np.empty((n, 3, 3))
+            s[:, 0, 0], s[:, 1, 1], s[:, 2, 2] = S0[:, 0], S0[:, 1], S0[:, 2]
+            s[:, 0, 1] = s[:, 1, 0] = S1[:, 2]
+            s[:, 0, 2] = s[:, 2, 0] = S1[:, 1]
+            s[:, 1, 2] = s[:, 2, 1] = S1[:, 0]
+            geo = np.einsum('ejp,epq,ekq->ejk', DN, s, DN)
+            KT += (Jdet[:, None, None] * geo)[:, :, :, None, None] * np.eye(3)[None, None, None]
+        return KT, KM
+
+    def Get_MatrixKN(self, U):
+        """FEM_model_bsr.py:134-145: (KT, KM) as CSR after InstallMatrixKN (:178-191) and the
+        penalty on both (ModifyMatrixK, :248-259)."""
+        nnzb = int(self.P.SmNode[-1])
+        VT = np.zeros((nnzb, 3, 3))
+        VM = np.zeros((nnzb, 3, 3))
+        for e0 in range(0, self.E, self.chunk):
+            e1 = min(self.E, e0 + self.chunk)
+            KT, KM = self.element_KN(e0, e1, np.asarray(U).reshape(-1, 3))
+            np.add.at(VT, self.slot[e0:e1].ravel(), KT.reshape(-1, 3, 3))
+            np.add.at(VM, self.slot[e0:e1].ravel(), KM.reshape(-1, 3, 3))
+        self._penalty(VT)
+        self._penalty(VM)
+        n = 3 * self.N
+        mk = lambda V: sp.bsr_matrix((V, np.asarray(self.P.ReNode), np.asarray(self.P.SmNode)),  # noqa: E731
+                                     shape=(n, n), dtype=np.float64).tocsr()
+        return mk(VT), mk(VM)
+
     # -- assembly ---------------------------------------------------------------
     def ValKT(self):
         """InstallMatrixKL scatter (FEM_model_bsr.py:163-175) + ModifyMatrixK (:248-259)."""

@@ -63,3 +63,24 @@ def bj_pcg(K, F, rtol=1e-10, maxit=100000):
         rz = rz_new
         it += 1
     return x, it, time.perf_counter() - t
+
+
+def newton_large_displacement(OM, F, max_errs=1e-4, max_iters=20):
+    """The large-displacement iteration of SOLVE_static.py:41-75 with exact (SuperLU) solves:
+    KT, KM at U (OracleModel.Get_MatrixKN), RF = KM U - F, stop at ||RF|| / ||F|| <= max_errs
+    or after max_iters steps, else U -= KT^-1 RF.  (SOLVE_static.py:72 solves with F; the
+    Newton-Raphson step uses RF.)  Returns (U, relative residuals)."""
+    F = np.asarray(F, dtype=np.float64)
+    U = np.zeros_like(F)
+    res = []
+    step = 0
+    while True:
+        KT, KM = OM.Get_MatrixKN(U.reshape(-1, 3))
+        RF = KM @ U - F
+        err = np.linalg.norm(RF) / np.linalg.norm(F)
+        res.append(err)
+        if err <= max_errs or step == max_iters:
+            break
+        U = U - spla.spsolve(sp.csc_matrix(KT), RF)
+        step += 1
+    return U, res
