@@ -8,10 +8,11 @@
 // element-size quantities) and only the outputs are formed in FP64 (integer assembly of
 // the double nearest below hi + lo).
 //
-//  k_hex8_element_dd -- 8 threads per element, 16 elements per CTA, 4 CTAs per SM:
-//     phase A per Gauss point (J, adjugate, det, 1/det, R_a = dN_a/dxi . adj J, R_a/det,
-//     centrifugal density), phase B per node pair (Gram P_ab -> K_ab, M_ab) and per corner
-//     (F_a).  Only R and R/det live in shared memory (55.5 KB per CTA); corner coordinates,
+//  k_hex8_element_dd -- 8 threads per element, 16 elements per CTA, 6 CTAs per SM:
+//     phase A per Gauss point (J, adjugate, det, R_a = dN_a/dxi . adj J, the scaled
+//     S_a = R_a / sqrt|det|, centrifugal density), phase B per node pair (Gram
+//     P_ab = sum_g sign(det_g) S_a S_b^T = sum_g R_a R_b^T / det_g -> K_ab, M_ab) and per
+//     corner (F_a).  Only S lives in shared memory (29 KB per CTA); corner coordinates,
 //     det and the load densities move between the 8 threads of an element by warp
 //     shuffles.  Output: one 672-byte chunk per (element, corner a) -- the 8 blocks
 //     K_e(a, b) with M_e(a, b) and F_e(a) -- stored at the position of (e, a) in the
@@ -85,15 +86,14 @@ struct ElemDdSmem {
     float2 dnr[8][8][3];
     float2 nr[8][8];
     float2 nn[36][8];
-    float2 R[kEpc][8][kRPad];
-    float2 Rs[kEpc][8][kRPad];
+    float2 R[kEpc][8][kRPad];  // S_a = R_a / sqrt|det| per Gauss point
 };
 
 __device__ __forceinline__ dd shfl_dd(dd v, int src) {
     return dd{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
 }
 
-__global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemDdParams p) {
+__global__ void __launch_bounds__(kElemThreads, 6) k_hex8_element_dd(const ElemDdParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ElemDdSmem& s = *reinterpret_cast<ElemDdSmem*>(smem_raw);
     const int tid = threadIdx.x;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemD
     acc_fma(da, J[1][0], A[0][1]);
     acc_fma(da, J[2][0], A[0][2]);
     const dd det = acc_value(da);
-    const dd inv = dd_rcp(det);
+    const dd isq = dd_rcp(dd_sqrt(dd_abs(det)));
 #pragma unroll 1
     for (int a = 0; a < 8; ++a)
 #pragma unroll
@@ -176,9 +176,7 @@ __global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemD
             acc_fma(acc, ld(s.dnr[g][a][0]), A[0][i]);
             acc_fma(acc, ld(s.dnr[g][a][1]), A[1][i]);
             acc_fma(acc, ld(s.dnr[g][a][2]), A[2][i]);
-            const dd r = acc_value(acc);
-            s.R[el][g][3 * a + i] = st(r);
-            s.Rs[el][g][3 * a + i] = st(dd_mul(r, inv));
+            s.R[el][g][3 * a + i] = st(dd_mul(acc_value(acc), isq));
         }
     dd cg[3];  // DE det f(x_g): centrifugal load density at this Gauss point
     {
@@ -218,14 +216,16 @@ __global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemD
 #pragma unroll 1
         for (int gg = 0; gg < 8; ++gg) {
             const dd r0 = ld(s.R[el][gg][3 * a]), r1 = ld(s.R[el][gg][3 * a + 1]), r2 = ld(s.R[el][gg][3 * a + 2]);
-            const dd q0 = ld(s.Rs[el][gg][3 * a]), q1 = ld(s.Rs[el][gg][3 * a + 1]), q2 = ld(s.Rs[el][gg][3 * a + 2]);
+            const dd dg = shfl_dd(det, base + gg);
+            const bool ng = dg.hi < 0.f;
+            const dd q0 = ng ? dd_neg(r0) : r0, q1 = ng ? dd_neg(r1) : r1, q2 = ng ? dd_neg(r2) : r2;
             acc_fma(P00, q0, r0);
             acc_fma(P11, q1, r1);
             acc_fma(P22, q2, r2);
             acc_fma(P01, q0, r1);
             acc_fma(P02, q0, r2);
             acc_fma(P12, q1, r2);
-            acc_fma(m, shfl_dd(det, base + gg), ld(s.nn[pi][gg]));
+            acc_fma(m, dg, ld(s.nn[pi][gg]));
         }
         const dd p00 = acc_value(P00), p11 = acc_value(P11), p22 = acc_value(P22);
         auto diag = [&](dd pp, dd qq, dd rr) {
@@ -262,16 +262,19 @@ __global__ void __launch_bounds__(kElemThreads, 4) k_hex8_element_dd(const ElemD
 #pragma unroll 1
         for (int gg = 0; gg < 8; ++gg) {
             dd qa[3], rb[3];
+            const dd dg = shfl_dd(det, base + gg);
+            const bool ng = dg.hi < 0.f;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                qa[i] = ld(s.Rs[el][gg][3 * a + i]);
+                const dd sa = ld(s.R[el][gg][3 * a + i]);
+                qa[i] = ng ? dd_neg(sa) : sa;
                 rb[i] = ld(s.R[el][gg][3 * b + i]);
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) acc_fma(P[i][k], qa[i], rb[k]);
-            acc_fma(m, shfl_dd(det, base + gg), ld(s.nn[pi][gg]));
+            acc_fma(m, dg, ld(s.nn[pi][gg]));
         }
         const int pos_a = __shfl_sync(0xffffffffu, pos, base + a);
         const int pos_b = __shfl_sync(0xffffffffu, pos, base + b);
