@@ -79,6 +79,17 @@ class FemPcgStats(ctypes.Structure):
                 ("time_ms", c_double)]
 
 
+class FemAmgOpts(ctypes.Structure):
+    _fields_ = [("theta", c_double), ("max_levels", c_int), ("max_coarse", c_int), ("smooth", c_int),
+                ("eig_steps", c_int), ("pre_degree", c_int), ("post_degree", c_int), ("cheb_upper", c_double),
+                ("cheb_ratio", c_double)]
+
+
+class FemAmgLevelInfo(ctypes.Structure):
+    _fields_ = [("n", c_int64), ("b", c_int), ("nnzb_A", c_int64), ("nnzb_P", c_int64), ("lmax", c_double),
+                ("omega", c_double), ("setup_s", c_double)]
+
+
 class FemMlp(ctypes.Structure):
     _fields_ = [("W1", c_void_p), ("b1", c_void_p), ("W2", c_void_p), ("b2", c_void_p), ("W3", c_void_p),
                 ("b3", c_void_p)]
@@ -126,6 +137,18 @@ SIGNATURES = {
     "fem_pcg_workspace_bytes": (c_size_t, [c_int64, c_int, c_int]),
     "fem_pcg_solve": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,
                               ctypes.POINTER(FemPcgOpts), ctypes.POINTER(FemPcgStats), c_void_p, c_size_t, c_void_p]),
+    "fem_amg_default_opts": (None, [ctypes.POINTER(FemAmgOpts)]),
+    "fem_amg_setup": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(FemAmgOpts),
+                              ctypes.POINTER(c_void_p)]),
+    "fem_amg_upload": (c_int, [c_void_p, c_void_p]),
+    "fem_amg_destroy": (None, [c_void_p]),
+    "fem_amg_num_levels": (c_int, [c_void_p]),
+    "fem_amg_get_level": (c_int, [c_void_p, c_int, ctypes.POINTER(FemAmgLevelInfo)]),
+    "fem_amg_export": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fem_amg_vcycle": (c_int, [c_void_p, ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_void_p]),
+    "fem_pcg_solve_amg": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,
+                                  ctypes.POINTER(FemPcgOpts), ctypes.POINTER(FemPcgStats), c_void_p, c_size_t,
+                                  c_void_p]),
     "fem_mlp_nparams": (c_int, []),
     "fem_precond_cholesky": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p]),
     "fem_precond_features": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

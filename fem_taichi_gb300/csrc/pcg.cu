@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "amg.cuh"
 #include "pcg.cuh"
 
 namespace fem {
@@ -220,6 +221,149 @@ __global__ void __launch_bounds__(kThreads) k_update(int64_t n, const T* __restr
     }
 }
 
+// ---- multigrid-preconditioned iteration: the preconditioner is a V-cycle launched between
+// k_update_r and k_rz, so r.z and beta move to a kernel of their own.  In the FP64 iteration
+// the (FP32) cycle reads an FP32 copy of r written by k_update_r and k_rz widens its output;
+// beta then takes the flexible (Polak-Ribiere) form beta = z_new.(r_new - r_old) / rz_old =
+// -alpha q.z_new / rz_old, which tolerates the cycle's FP32 rounding. ----------------------
+// x = 0, r = b (r32 = b when given); rr -> state (bb, tol2, active).
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_init_r(int64_t nv, const T* __restrict__ b, T* x, T* r, float* r32,
+                                                      double* part, PcgState* st, double rtol, int maxit) {
+    double v[1];
+    Dot<T> d_rr;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ((nv + 31) / 32) * 32;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        if (e < nv) {
+            const T b0 = b[e];
+            x[e] = T(0);
+            r[e] = b0;
+            if (r32) r32[e] = float(b0);
+            d_rr.add(b0, b0);
+        }
+    }
+    v[0] = d_rr.value();
+    if (!block_partials<R, 1>(v, part, &st->ticket)) return;
+    __shared__ double tot[1][kMaxR];
+    last_block_totals<R, 1>(part, gridDim.x, tot);
+    if (threadIdx.x == 0) {
+        int any = 0, status = FEM_OK;
+        for (int k = 0; k < kMaxR; ++k) {
+            const double rr = k < R ? tot[0][k] : 0.0;
+            if (!isfinite(rr)) status = FEM_ERR_BREAKDOWN;
+            st->rz[k] = 0.0;
+            st->bb[k] = rr;
+            st->rr[k] = rr;
+            st->tol2[k] = rtol * rtol * rr;
+            st->active[k] = (k < R && isfinite(rr) && rr > 0.0) ? 1 : 0;
+            st->beta[k] = 0.0;
+            st->alpha[k] = 0.0;
+            st->iters[k] = 0;
+            any |= st->active[k];
+        }
+        st->it = 0;
+        st->done = !any;
+        st->status = status;
+        st->maxit = maxit;
+        st->ticket = 0;
+    }
+}
+
+// x += alpha p; r -= alpha q (r32 = r when given); rr -> convergence and iteration count.
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_update_r(int64_t nv, const T* __restrict__ p, const T* __restrict__ q,
+                                                        T* x, T* r, float* r32, double* part, PcgState* st) {
+    if (st->done) return;
+    double v[1];
+    Dot<T> d_rr;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ((nv + 31) / 32) * 32;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        if (e < nv) {
+            const T a = T(st->alpha[e % R]);
+            x[e] += a * p[e];
+            const T r0 = r[e] - a * q[e];
+            r[e] = r0;
+            if (r32) r32[e] = float(r0);
+            d_rr.add(r0, r0);
+        }
+    }
+    v[0] = d_rr.value();
+    if (block_partials<R, 1>(v, part, &st->ticket)) {
+        __shared__ double tot[1][kMaxR];
+        last_block_totals<R, 1>(part, gridDim.x, tot);
+        const int k = threadIdx.x;
+        if (k < R && st->active[k]) {
+            const double rr = tot[0][k];
+            st->rr[k] = rr;
+            st->iters[k] += 1;
+            if (!(rr > st->tol2[k])) st->active[k] = 0;
+            if (!isfinite(rr)) {
+                st->active[k] = 0;
+                st->status = FEM_ERR_BREAKDOWN;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int kk = 0; kk < R; ++kk) any |= st->active[kk];
+            st->it += 1;
+            if (any && st->it >= st->maxit) {
+                st->status = st->status ? st->status : FEM_ERR_MAXITER;
+                any = 0;
+            }
+            st->done = !any;
+            st->ticket = 0;
+        }
+    }
+}
+
+// z = z32 when given (FP64 iteration); r.z (and q.z when q is given) -> beta, rz.
+template <typename T, int R>
+__global__ void __launch_bounds__(kThreads) k_rz(int64_t nv, const T* __restrict__ r, T* z, const float* z32,
+                                                  const T* __restrict__ q, double* part, PcgState* st) {
+    if (st->done) return;
+    double v[2];
+    Dot<T> d_rz, d_qz;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ((nv + 31) / 32) * 32;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        if (e < nv) {
+            T ze;
+            if (z32) {
+                ze = T(z32[e]);
+                z[e] = ze;
+            } else {
+                ze = z[e];
+            }
+            d_rz.add(r[e], ze);
+            if (q) d_qz.add(q[e], ze);
+        }
+    }
+    v[0] = d_rz.value();
+    v[1] = d_qz.value();
+    if (block_partials<R, 2>(v, part, &st->ticket)) {
+        __shared__ double tot[2][kMaxR];
+        last_block_totals<R, 2>(part, gridDim.x, tot);
+        const int k = threadIdx.x;
+        if (k < R && st->active[k]) {
+            const double rz = tot[0][k];
+            if (rz > 0.0 && isfinite(rz)) {
+                if (st->it > 0) st->beta[k] = q ? -st->alpha[k] * tot[1][k] / st->rz[k] : rz / st->rz[k];
+                st->rz[k] = rz;
+            } else {
+                st->active[k] = 0;
+                st->status = isfinite(rz) ? FEM_ERR_NOT_SPD : FEM_ERR_BREAKDOWN;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int kk = 0; kk < R; ++kk) any |= st->active[kk];
+            st->done = !any;
+            st->ticket = 0;
+        }
+    }
+}
+
 // ---- FP64 refinement helpers --------------------------------------------------------------
 // r = b - y (y = A u computed by the SpMV), norms of r per RHS -> st->norm2.
 template <int R>
@@ -345,18 +489,19 @@ struct InnerResult {
     int iters, status;
 };
 
-// Runs PCG on (A, M) with right-hand side b into x; vectors r z p q are workspace.
-template <typename T, int R>
-int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
-             double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res) {
-    k_init<T, R><<<vec_grid(A.n * R), kThreads, 0, s>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
-    FEM_LAUNCH_CHECK("k_init");
+// Initialises the solver state (init(s)), then runs `unroll` iterations at a time
+// (iters(count, s), replayed as one CUDA graph when use_graph) until the state says done.
+template <typename Init, typename Iters>
+int pcg_drive(const Init& init, const Iters& iters, PcgState* st, int maxit, int use_graph, int unroll,
+              cudaStream_t s, InnerResult* res) {
+    int rc0 = init(s);
+    if (rc0) return rc0;
     unroll = std::max(1, std::min(unroll, 256));
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
         cudaGraph_t g = nullptr;
         FEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int rc = launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, unroll, s);
+        int rc = iters(unroll, s);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc) return rc;
         FEM_CUDA(ce);
@@ -371,7 +516,7 @@ int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p
         if (exec) {
             rc = cuda_status(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
         } else {
-            rc = launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, unroll, s);
+            rc = iters(unroll, s);
         }
         if (rc) break;
         launched += unroll;
@@ -387,8 +532,62 @@ int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p
     return FEM_OK;
 }
 
+// Runs PCG on (A, M) with right-hand side b into x; vectors r z p q are workspace.
+template <typename T, int R>
+int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
+             double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res) {
+    auto init = [&](cudaStream_t ss) -> int {
+        k_init<T, R><<<vec_grid(A.n * R), kThreads, 0, ss>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
+        FEM_LAUNCH_CHECK("k_init");
+        return FEM_OK;
+    };
+    auto iters = [&](int count, cudaStream_t ss) -> int {
+        return launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, count, ss);
+    };
+    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res);
+}
+
+// The same with the multigrid V-cycle as the preconditioner.  T = float: the FP32 inner
+// solve (A the FP32 matrix, which the cycle also uses).  T = double: FP64 vectors and
+// products with A, the cycle in FP32 on A32 through the handle's FP32 copies of r and z.
+template <typename T, int R>
+int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, const T* b, T* x, T* r, T* z, T* p,
+                 T* q, double* part, PcgState* st, double rtol, int maxit, int variant, int use_graph, int unroll,
+                 cudaStream_t s, InnerResult* res) {
+    const int64_t nv = 3 * A.n * R;
+    const unsigned gv = vec_grid(nv);
+    constexpr bool f64 = sizeof(T) == 8;
+    float* r32 = f64 ? amg->r32 : nullptr;
+    float* z32 = f64 ? amg->z32 : nullptr;
+    const float* rin = f64 ? r32 : reinterpret_cast<const float*>(r);
+    float* zout = f64 ? z32 : reinterpret_cast<float*>(z);
+    const T* qflex = f64 ? q : nullptr;
+    auto init = [&](cudaStream_t ss) -> int {
+        k_init_r<T, R><<<gv, kThreads, 0, ss>>>(nv, b, x, r, r32, part, st, rtol, maxit);
+        FEM_LAUNCH_CHECK("k_init_r");
+        int rc = amg::vcycle(amg, A32, rin, zout, st, R, ss);
+        if (rc) return rc;
+        k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, nullptr, part, st);
+        FEM_LAUNCH_CHECK("k_rz");
+        return FEM_OK;
+    };
+    auto iters = [&](int count, cudaStream_t ss) -> int {
+        for (int i = 0; i < count; ++i) {
+            k_p_update<T, R><<<gv, kThreads, 0, ss>>>(nv, z, p, st);
+            launch_spmv_pq<T, R>(A, p, q, part, st, variant, ss);
+            k_update_r<T, R><<<gv, kThreads, 0, ss>>>(nv, p, q, x, r, r32, part, st);
+            int rc = amg::vcycle(amg, A32, rin, zout, st, R, ss);
+            if (rc) return rc;
+            k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, qflex, part, st);
+        }
+        FEM_LAUNCH_CHECK("pcg iteration (amg)");
+        return FEM_OK;
+    };
+    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res);
+}
+
 template <int R>
-int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const double* F, double* U,
+int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* amg, const double* F, double* U,
             const fem_pcg_opts* o, fem_pcg_stats* out, unsigned char* ws, cudaStream_t s) {
     const int64_t n = A64->n_brow;
     const int64_t nv = 3 * n * R;
@@ -429,8 +628,16 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
         double* z = reinterpret_cast<double*>(ws + L.v64[1]);
         double* p = reinterpret_cast<double*>(ws + L.v64[2]);
         double* q = reinterpret_cast<double*>(ws + L.v64[3]);
-        int rc = pcg_core<double, R>(K64, M64, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
+        int rc;
+        if (amg) {
+            const BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
+                                     rsoa_kind(A32->layout)};
+            rc = pcg_core_amg<double, R>(K64, K32, amg, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
+                                         o->use_graph, o->unroll, s, &ir);
+        } else {
+            rc = pcg_core<double, R>(K64, M64, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
                                      o->use_graph, o->unroll, s, &ir);
+        }
         if (rc) return rc;
         total_iters = ir.iters;
         outer = 1;
@@ -450,7 +657,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
         float* qq = reinterpret_cast<float*>(ws + L.v32[5]);
         float* M32 = reinterpret_cast<float*>(ws + L.m32);
         double* scale = reinterpret_cast<double*>(ws + L.scale);
-        int rc = fem_convert_f64_to_f32(M64, M32, 9 * n, s);
+        int rc = amg ? FEM_OK : fem_convert_f64_to_f32(M64, M32, 9 * n, s);
         if (rc) return rc;
         k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, U);
         FEM_LAUNCH_CHECK("k_zero");
@@ -478,8 +685,14 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, const dou
             FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
             k_scale_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, r64, scale, b32);
             FEM_LAUNCH_CHECK("k_scale_cast");
-            rc = pcg_core<float, R>(K32, M32, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
-                                    std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll, s, &ir);
+            if (amg)
+                rc = pcg_core_amg<float, R>(K32, K32, amg, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
+                                            std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll,
+                                            s, &ir);
+            else
+                rc = pcg_core<float, R>(K32, M32, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
+                                        std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll, s,
+                                        &ir);
             if (rc) return rc;
             total_iters += ir.iters;
             if (ir.status == FEM_ERR_BREAKDOWN || ir.status == FEM_ERR_NOT_SPD) {
@@ -519,17 +732,20 @@ extern "C" size_t fem_pcg_workspace_bytes(int64_t n_brow, int nrhs, int mixed) {
     return layout(n_brow, nrhs, mixed ? 1 : 0).total;
 }
 
-extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F,
-                             double* U, const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace,
-                             size_t workspace_bytes, void* stream) {
-    FEM_REQUIRE(A64 && opts && stats && precond && F && U, "NULL argument");
+namespace fem {
+namespace {
+
+int run_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, fem_amg* amg, const double* F,
+              double* U, const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
+              void* stream) {
+    FEM_REQUIRE(A64 && opts && stats && (precond || amg) && F && U, "NULL argument");
     FEM_REQUIRE(A64->dtype == FEM_F64 && A64->n_brow > 0 && A64->indptr && A64->indices && A64->vals,
                 "A64 must be a non-empty FP64 BSR matrix");
     FEM_REQUIRE(A64->layout == FEM_LAYOUT_BSR || A64->layout == FEM_LAYOUT_RSOA, "A64: layout must be BSR or RSOA");
     const int R = opts->nrhs;
     FEM_REQUIRE(R == 1 || R == 2 || R == 4 || R == 8 || R == 16 || R == 32, "nrhs must be 1, 2, 4, 8, 16 or 32");
     FEM_REQUIRE(opts->rtol > 0 && opts->maxit > 0, "rtol and maxit must be positive");
-    if (opts->mixed) {
+    if (opts->mixed || amg) {
         FEM_REQUIRE(A32 && A32->dtype == FEM_F32 && A32->n_brow == A64->n_brow && A32->vals && A32->indptr &&
                         A32->indices,
                     "mixed precision needs the FP32 copy of the matrix (A32)");
@@ -538,7 +754,11 @@ extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const doubl
         FEM_REQUIRE(A32->layout != FEM_LAYOUT_RSOA4 ||
                         ((reinterpret_cast<uintptr_t>(A32->vals) | reinterpret_cast<uintptr_t>(A32->indices)) & 15u) == 0,
                     "A32: FEM_LAYOUT_RSOA4 arrays must be 16-byte aligned");
-        FEM_REQUIRE(opts->inner_rtol > 0 && opts->inner_rtol < 1, "inner_rtol must lie in (0, 1)");
+        FEM_REQUIRE(!opts->mixed || (opts->inner_rtol > 0 && opts->inner_rtol < 1), "inner_rtol must lie in (0, 1)");
+    }
+    if (amg) {
+        FEM_REQUIRE(amg->uploaded, "call fem_amg_upload first");
+        FEM_REQUIRE(amg->lv[0].n == A64->n_brow, "the AMG hierarchy belongs to a matrix of another size");
     }
     const Layout L = layout(A64->n_brow, R, opts->mixed);
     if (!workspace || workspace_bytes < L.total) {
@@ -546,6 +766,11 @@ extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const doubl
         return FEM_ERR_WORKSPACE;
     }
     FEM_REQUIRE(aligned16(workspace), "workspace must be 16-byte aligned");
+    if (amg) {
+        // per-level vectors are allocated before any capture
+        int rc = amg::ensure_vectors(amg, R);
+        if (rc) return rc;
+    }
     // Work on a private stream ordered after / before the caller's stream (graph capture
     // is not allowed on the legacy default stream).
     cudaStream_t caller = as_stream(stream), s = nullptr;
@@ -569,12 +794,12 @@ extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const doubl
         if ((rc = cuda_status(cudaEventRecord(t0, s), "record"))) break;
         unsigned char* ws = static_cast<unsigned char*>(workspace);
         switch (R) {
-            case 1: rc = solve_r<1>(A64, A32, precond, F, U, opts, stats, ws, s); break;
-            case 2: rc = solve_r<2>(A64, A32, precond, F, U, opts, stats, ws, s); break;
-            case 4: rc = solve_r<4>(A64, A32, precond, F, U, opts, stats, ws, s); break;
-            case 8: rc = solve_r<8>(A64, A32, precond, F, U, opts, stats, ws, s); break;
-            case 16: rc = solve_r<16>(A64, A32, precond, F, U, opts, stats, ws, s); break;
-            default: rc = solve_r<32>(A64, A32, precond, F, U, opts, stats, ws, s); break;
+            case 1: rc = solve_r<1>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
+            case 2: rc = solve_r<2>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
+            case 4: rc = solve_r<4>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
+            case 8: rc = solve_r<8>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
+            case 16: rc = solve_r<16>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
+            default: rc = solve_r<32>(A64, A32, precond, amg, F, U, opts, stats, ws, s); break;
         }
         if (rc) break;
         if ((rc = cuda_status(cudaEventRecord(t1, s), "record"))) break;
@@ -588,4 +813,21 @@ extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const doubl
     if (rc) cudaStreamSynchronize(s);
     cleanup();
     return rc;
+}
+
+}  // namespace
+}  // namespace fem
+
+extern "C" int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F,
+                             double* U, const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    FEM_REQUIRE(precond, "NULL argument");
+    return run_solve(A64, A32, precond, nullptr, F, U, opts, stats, workspace, workspace_bytes, stream);
+}
+
+extern "C" int fem_pcg_solve_amg(const fem_bsr* A64, const fem_bsr* A32, fem_amg* amg, const double* F, double* U,
+                                 const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+    FEM_REQUIRE(amg, "NULL argument");
+    return run_solve(A64, A32, nullptr, amg, F, U, opts, stats, workspace, workspace_bytes, stream);
 }

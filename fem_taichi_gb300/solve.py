@@ -8,7 +8,14 @@ the block-preconditioned CG of ``libfemgb.so`` (``fem_pcg_solve``):
 * ``mixed=True``: FP32 SpMV / FP32 preconditioner inner PCG inside FP64 iterative
   refinement (true residual r = F - K u in FP64);
 * up to 32 right-hand sides in one solve (lockstep PCG, BSR SpMM);
-* iterations replayed as CUDA graphs; SpMV launch shape chosen by the autotuner.
+* iterations replayed as CUDA graphs; SpMV launch shape chosen by the autotuner;
+* ``precond="amg"``: a smoothed-aggregation multigrid V-cycle (rigid-body modes, Chebyshev
+  smoothing, FP32) preconditions the solve, for meshes where block-diagonal preconditioners
+  stall (``fem_amg_setup`` / ``fem_pcg_solve_amg``).  ``mixed=True`` runs it inside the FP32
+  inner solve of the refinement loop; ``mixed=False`` runs FP64 flexible CG (FP64 products
+  with K) around the FP32 cycle, which also converges when the condition number is beyond
+  FP32 refinement (kappa >~ 1e7, e.g. slender cantilevers); a mixed solve that stalls is
+  repeated that way.
 
 ``Static_solver(Model, Qtype=0).Solve_cpu(max_errs, max_iters)`` keeps the reference's
 signature and return value (U, (3N,) float64) but runs the GPU solve to a tight tolerance
@@ -22,7 +29,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import FemBsr, FemPcgOpts, FemPcgStats, FEM_F32, FEM_F64
+from ._lib import FemAmgLevelInfo, FemAmgOpts, FemBsr, FemPcgOpts, FemPcgStats, FEM_F32, FEM_F64
 from .model import _dptr, _stream
 
 SUPPORTED_NRHS = (1, 2, 4, 8, 16, 32)
@@ -36,6 +43,82 @@ def padded_nrhs(r: int) -> int:
         if r <= s:
             return s
     raise ValueError("at most 32 right-hand sides per solve")
+
+
+class AmgHierarchy:
+    """Owner of a ``fem_amg`` hierarchy (host setup + device copy) for one matrix.
+
+    Built from the FP64 BSR matrix of a ``DeviceSystem`` (copied to the host for the setup)
+    and the node coordinates (rigid-body modes).  ``opts`` overrides fields of
+    ``fem_amg_default_opts``."""
+
+    def __init__(self, lib, n, indptr, indices, vals, xyz, stream=None, **opts):
+        import time
+        self.lib = lib
+        o = FemAmgOpts()
+        lib.fem_amg_default_opts(ctypes.byref(o))
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise ValueError(f"unknown AMG option {k}")
+            setattr(o, k, v)
+        self.opts = o
+        ip = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix = np.ascontiguousarray(indices, dtype=np.int32)
+        va = np.ascontiguousarray(vals, dtype=np.float64)
+        xy = np.ascontiguousarray(xyz, dtype=np.float64).reshape(n, 3)
+        h = ctypes.c_void_p()
+        t0 = time.perf_counter()
+        _lib.check(lib.fem_amg_setup(n, ip.ctypes.data, ix.ctypes.data, va.ctypes.data, xy.ctypes.data,
+                                     ctypes.byref(o), ctypes.byref(h)), "fem_amg_setup")
+        self.h = h
+        self.setup_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        if stream is not None:
+            _lib.check(lib.fem_amg_upload(self.h, stream), "fem_amg_upload")
+        self.upload_s = time.perf_counter() - t0
+
+    def levels(self):
+        out = []
+        for l in range(int(self.lib.fem_amg_num_levels(self.h))):
+            info = FemAmgLevelInfo()
+            _lib.check(self.lib.fem_amg_get_level(self.h, l, ctypes.byref(info)), "fem_amg_get_level")
+            out.append({"n": info.n, "b": info.b, "nnzb_A": info.nnzb_A, "nnzb_P": info.nnzb_P,
+                        "lmax": info.lmax, "omega": info.omega, "setup_s": info.setup_s})
+        return out
+
+    def export(self, level, what):
+        """Host copy of one level's array (see fem_amg_export): a scipy BSR-like triple
+        (indptr, indices, blocks) for what in 0..2, else the value / index array."""
+        dims = (ctypes.c_int64 * 4)()
+        _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, None, None, None), "fem_amg_export")
+        rows, nnz, br, bc = (int(d) for d in dims)
+        if what <= 2:
+            ptr = np.zeros(rows + 1, dtype=np.int64)
+            col = np.zeros(max(nnz, 1), dtype=np.int32)
+            val = np.zeros(max(nnz, 1) * br * bc, dtype=np.float64)
+            _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, ptr.ctypes.data, col.ctypes.data,
+                                               val.ctypes.data), "fem_amg_export")
+            return ptr, col[:nnz], val[:nnz * br * bc].reshape(nnz, br, bc)
+        if what == 4:
+            idx = np.zeros(max(nnz, 1), dtype=np.int32)
+            _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, None, idx.ctypes.data, None),
+                       "fem_amg_export")
+            return idx[:nnz]
+        val = np.zeros(max(nnz, 1), dtype=np.float64)
+        _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, None, None, val.ctypes.data),
+                   "fem_amg_export")
+        return val[:nnz]
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.fem_amg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DeviceSystem:
@@ -58,6 +141,7 @@ class DeviceSystem:
         self._bj = None
         self._variant = {}
         self._ws = None
+        self._amg = None
 
     @property
     def stream(self):
@@ -93,6 +177,18 @@ class DeviceSystem:
                 raise _lib.FemError(_lib.FEM_ERR_NOT_SPD, f"{int(bad.item())} singular diagonal blocks")
             self._bj = bj
         return self._bj
+
+    def amg(self, **opts) -> AmgHierarchy:
+        """Smoothed-aggregation multigrid hierarchy of K (built once; ``opts`` as
+        ``fem_amg_opts``).  The setup runs on the host from a copy of K."""
+        if self._amg is None or opts:
+            P = self.model.Physics
+            xyz = self.model.mesh.xyz.cpu().numpy()
+            K = self.K64.reshape(-1).cpu().numpy()
+            if self._amg is not None:
+                self._amg.close()
+            self._amg = AmgHierarchy(self.lib, self.n, P.SmNode, P.ReNode, K, xyz, self.stream, **opts)
+        return self._amg
 
     def spmv(self, x: torch.Tensor, fp32=False, nrhs=1) -> torch.Tensor:
         A = self._A32 if fp32 else self.A64
@@ -130,8 +226,9 @@ class DeviceSystem:
               inner_rtol=1e-4, inner_maxit=20000, max_outer=40):
         """Solve K U = F.  F: device/host array (3N,) or (3N, R) (default: the assembled F).
 
-        precond: (N, 9) FP64 blocks (default block Jacobi).  Returns (U (3N,) or (3N, R)
-        device tensor, stats dict)."""
+        precond: (N, 9) FP64 blocks (default block Jacobi), or "amg" (multigrid V-cycle; with
+        mixed=True inside the FP32 inner solve, falling back to the FP64 flexible-CG form when
+        the refinement stalls).  Returns (U (3N,) or (3N, R) device tensor, stats dict)."""
         if F is None:
             F = self.F
         F = torch.as_tensor(F, dtype=torch.float64, device=self.device)
@@ -143,9 +240,15 @@ class DeviceSystem:
             F2 = torch.cat([F2, torch.zeros((3 * self.n, Rp - R), dtype=torch.float64, device=self.device)], 1)
         F2 = F2.contiguous()
         U = torch.empty_like(F2)
-        P = self.block_jacobi() if precond is None else torch.as_tensor(precond, dtype=torch.float64,
-                                                                         device=self.device).reshape(self.n, 9)
-        P = P.contiguous()
+        use_amg = isinstance(precond, str) and precond == "amg"
+        if use_amg:
+            amg = self.amg()
+            self.K32()
+            P = None
+        else:
+            P = self.block_jacobi() if precond is None else torch.as_tensor(precond, dtype=torch.float64,
+                                                                             device=self.device).reshape(self.n, 9)
+            P = P.contiguous()
         if mixed:
             self.K32()
         nbytes = int(self.lib.fem_pcg_workspace_bytes(self.n, Rp, int(mixed)))
@@ -155,13 +258,24 @@ class DeviceSystem:
                           int(max_outer), int(use_graph), int(unroll), self.variant(False, Rp),
                           self.variant(True, Rp) if mixed else 0)
         st = FemPcgStats()
-        A32 = ctypes.byref(self._A32) if mixed else None
-        _lib.check(self.lib.fem_pcg_solve(ctypes.byref(self.A64), A32, _dptr(P), _dptr(F2), _dptr(U),
-                                          ctypes.byref(opts), ctypes.byref(st), _dptr(self._ws), self._ws.numel(),
-                                          self.stream), "fem_pcg_solve")
+        A32 = ctypes.byref(self._A32) if (mixed or use_amg) else None
+        if use_amg:
+            _lib.check(self.lib.fem_pcg_solve_amg(ctypes.byref(self.A64), A32, amg.h, _dptr(F2), _dptr(U),
+                                                  ctypes.byref(opts), ctypes.byref(st), _dptr(self._ws),
+                                                  self._ws.numel(), self.stream), "fem_pcg_solve_amg")
+        else:
+            _lib.check(self.lib.fem_pcg_solve(ctypes.byref(self.A64), A32, _dptr(P), _dptr(F2), _dptr(U),
+                                              ctypes.byref(opts), ctypes.byref(st), _dptr(self._ws),
+                                              self._ws.numel(), self.stream), "fem_pcg_solve")
         stats = {"status": st.status, "status_text": _STATUS.get(st.status, str(st.status)),
                  "iterations": st.iterations, "outer": st.outer, "relres": st.relres, "time_ms": st.time_ms,
-                 "nrhs": R, "mixed": bool(mixed)}
+                 "nrhs": R, "mixed": bool(mixed), "precond": "amg" if use_amg else "block"}
+        if use_amg and mixed and st.status == _lib.FEM_ERR_NOT_CONVERGED:
+            # FP32 refinement stalled (condition number beyond FP32): FP64 flexible CG instead
+            U2, st2 = self.solve(F=F if squeeze else F2[:, :R], rtol=rtol, maxit=maxit, mixed=False, precond="amg",
+                                 use_graph=use_graph, unroll=unroll)
+            st2["fallback_from"] = stats
+            return U2, st2
         U = U[:, :R]
         return (U.reshape(-1) if squeeze else U), stats
 
@@ -219,9 +333,9 @@ class Static_solver:
         return U.cpu().numpy()
 
     def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, **kw):
-        """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'learned' (uses
-        ``self.Model.learned_precond`` (N, 9) if set, falling back to block Jacobi when the
-        learned solve does not converge) or an (N, 9) array."""
+        """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'amg' (multigrid
+        V-cycle), 'learned' (uses ``self.Model.learned_precond`` (N, 9) if set, falling back to
+        block Jacobi when the learned solve does not converge) or an (N, 9) array."""
         if self.Qtype != 0:
             raise ValueError("Solve_gpu is the linear solve; Qtype=1 uses Solve_cpu / Solve_nonlinear")
         S = self._system()
@@ -233,8 +347,10 @@ class Static_solver:
                 if P is None:
                     raise ValueError("no learned preconditioner attached to the model (Model.learned_precond)")
                 fallback = True
+            elif precond == "amg":
+                P = "amg"
             elif precond != "bj":
-                raise ValueError("precond must be 'bj', 'learned' or an (N, 9) array")
+                raise ValueError("precond must be 'bj', 'amg', 'learned' or an (N, 9) array")
         else:
             P = precond
         U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P, **kw)

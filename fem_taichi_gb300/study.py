@@ -11,7 +11,10 @@
 
 Every solution is compared with an FP64 reference solve of the same system (FP32-inner /
 FP64-refinement PCG driven to a relative residual of 1e-13; its own error is estimated by a
-second solve at 1e-12), standing in for the reference's MKL Pardiso.
+second solve at 1e-12), standing in for the reference's MKL Pardiso.  The reference solve
+uses block Jacobi on c3 / c4 and the multigrid preconditioner on c5, where block-diagonal
+preconditioners do not converge.  ``mixed_amg`` rows add the multigrid preconditioner
+(host setup time reported separately as ``amg_setup_s``).
 """
 from __future__ import annotations
 
@@ -79,12 +82,26 @@ def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda"):
                  "loss_end": hist[-1], "data_s": t_data, "train_s": t_train}
 
 
-def reference_solution(S: DeviceSystem, F=None):
-    """FP64 reference (refinement to 1e-13) and its estimated relative error."""
-    U1, s1 = S.solve(F=F, rtol=1e-13, mixed=True, maxit=200000, inner_maxit=50000, max_outer=60)
-    U2, s2 = S.solve(F=F, rtol=1e-12, mixed=True, maxit=200000, inner_maxit=50000, max_outer=60)
+def reference_solution(S: DeviceSystem, F=None, precond=None, mixed=True, rtol=(1e-13, 1e-12)):
+    """FP64 reference (to rtol[0]) and its relative difference from a solve to rtol[1]."""
+    kw = dict(F=F, mixed=mixed, maxit=200000, inner_maxit=50000, max_outer=60, precond=precond)
+    U1, s1 = S.solve(rtol=rtol[0], **kw)
+    U2, s2 = S.solve(rtol=rtol[1], **kw)
     est = float(torch.linalg.norm(U1 - U2) / torch.linalg.norm(U1))
-    return U1, {"relres": s1["relres"], "status": s1["status"], "est_err_of_1e-12_solve": est}
+    return U1, {"relres": s1["relres"], "status": s1["status"], f"est_err_of_{rtol[1]:g}_solve": est,
+                "precond": precond or "block Jacobi", "mixed": s1["mixed"], "iterations": s1["iterations"]}
+
+
+def amg_setup(S: DeviceSystem, **opts):
+    """Builds the multigrid hierarchy of S (host setup + upload) and reports its cost."""
+    t = time.perf_counter()
+    H = S.amg(**opts)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t
+    lv = H.levels()
+    return {"setup_s": H.setup_s, "upload_s": H.upload_s, "wall_s": wall,
+            "levels": [(l["n"], l["b"], l["nnzb_A"] or None) for l in lv],
+            "operator_complexity": (S.nnzb * 9 + sum(l["nnzb_A"] * 36 for l in lv[1:])) / (S.nnzb * 9)}
 
 
 def relerr(U, Ur):
@@ -177,12 +194,15 @@ def c3_study(device="cuda", rtol=1e-10, peak_gbs=None):
     extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
     S = DeviceSystem(Model("c3", P, STEEL, device=device, extra_loads=extra))
     Ur, ref = reference_solution(S)
+    amg = amg_setup(S)
     rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
-                           ("mixed_bj", dict(rtol=rtol, mixed=True))])
+                           ("mixed_bj", dict(rtol=rtol, mixed=True)),
+                           ("mixed_amg", dict(rtol=rtol, mixed=True, precond="amg")),
+                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))])
     for r in rows:
         r["ms_per_iteration"] = 1e3 * r["wall_s"] / max(r["iterations"], 1)
     return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows,
-            "spmv": spmv_rates(S, peak_gbs=peak_gbs)}
+            "amg": amg, "spmv": spmv_rates(S, peak_gbs=peak_gbs)}
 
 
 def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
@@ -198,12 +218,15 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
     torch.cuda.synchronize()
     t_inf = time.perf_counter() - t
     Ur, ref = reference_solution(S)
+    amg = amg_setup(S)
     rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
                            ("mixed_bj", dict(rtol=rtol, mixed=True)),
                            ("mixed_learned", dict(rtol=rtol, mixed=True, precond=Pl)),
-                           ("fp64_learned", dict(rtol=rtol, mixed=False, precond=Pl))])
+                           ("fp64_learned", dict(rtol=rtol, mixed=False, precond=Pl)),
+                           ("mixed_amg", dict(rtol=rtol, mixed=True, precond="amg")),
+                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))])
     return {"workload": "c4 eval 160x160x20, 544,341 nodes", "training": info, "inference_s": t_inf,
-            "reference": ref, "solves": rows}, net
+            "reference": ref, "solves": rows, "amg": amg}, net
 
 
 def c5_system(device="cuda", nrhs=32, seed=5):
@@ -223,20 +246,33 @@ def c5_system(device="cuda", nrhs=32, seed=5):
     return S, Fm
 
 
-def c5_study(net, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3000):
-    """Capped: block-diagonal preconditioners need far more than ``maxit`` iterations on
-    this slender slab, so the study reports the residual reached within the cap."""
+def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3000, block_variants=True):
+    """32 right-hand sides on the slender twisted slab (condition number far beyond FP32
+    refinement).  The reference solve and the ``fp64_amg`` rows run FP64 flexible CG around
+    the FP32 multigrid cycle; block-diagonal preconditioners (capped at ``maxit`` iterations)
+    do not reach 1e-8 here and are reported with the error they reach."""
     S, Fm = c5_system(device, nrhs)
-    Pl = net.blocks(S)
-    U1, s1 = S.solve(F=Fm, rtol=1e-13, mixed=False, maxit=maxit)
-    Ur, ref = U1, {"relres": s1["relres"], "status": s1["status"], "note": f"FP64 PCG capped at {maxit}"}
-    variants = [("mixed_learned", dict(rtol=rtol, mixed=True, precond=Pl, maxit=maxit, inner_maxit=maxit)),
-                ("mixed_bj", dict(rtol=rtol, mixed=True, maxit=maxit, inner_maxit=maxit))]
-    if include_fp64:
-        variants.append(("fp64_bj", dict(rtol=rtol, mixed=False, maxit=maxit)))
-    rows = compare(S, Ur, variants, F=Fm)
+    amg = amg_setup(S)
+    Ur, ref = reference_solution(S, F=Fm, precond="amg", mixed=False, rtol=(1e-12, 1e-11))
+    variants = [("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg")),
+                ("fp64_amg_1rhs", dict(F=Fm[:, 0].contiguous(), rtol=rtol, mixed=False, precond="amg"))]
+    rows = []
+    for label, kw in variants:
+        F_ = kw.pop("F", Fm)
+        U, st = timed_solve(S, label, F=F_, **kw)
+        st["relerr"] = relerr(U, Ur if F_.dim() == 2 else Ur[:, 0])
+        st["meets_1e-8"] = bool(st["relerr"] <= 1e-8 and st["status"] == 0)
+        rows.append(st)
+    if block_variants:
+        bv = [("mixed_bj", dict(rtol=rtol, mixed=True, maxit=maxit, inner_maxit=maxit))]
+        if net is not None:
+            bv.insert(0, ("mixed_learned", dict(rtol=rtol, mixed=True, precond=net.blocks(S), maxit=maxit,
+                                                inner_maxit=maxit)))
+        if include_fp64:
+            bv.append(("fp64_bj", dict(rtol=rtol, mixed=False, maxit=maxit)))
+        rows += compare(S, Ur, bv, F=Fm)
     return {"workload": f"c5 twisted slab 1200x120x15, 2,325,136 nodes, {nrhs} RHS", "reference": ref,
-            "solves": rows}
+            "amg": amg, "solves": rows}
 
 
 def solve_probe(cfg="c3", iterations=40, device="cuda", variant64=None, variant32=None):

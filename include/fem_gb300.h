@@ -7,7 +7,9 @@
  * Every entry point returns an int status (FEM_OK == 0, negative on error) and never
  * throws; fem_last_error() returns a thread-local message for the last failure.
  * No entry point keeps global mutable state: callers own every buffer (outputs and
- * workspaces are caller-allocated; *_workspace_bytes() tells how much to allocate).
+ * workspaces are caller-allocated; *_workspace_bytes() tells how much to allocate).  The
+ * one object that owns device memory is the multigrid hierarchy (fem_amg), which the
+ * caller creates and destroys explicitly.
  *
  * Reference interfaces replaced (tianshao1992/FEM_taichi):
  *   fem_pattern_*          READ_physics.py:42-61       Read.pre_process (SmNode/ReNode/CoNode)
@@ -22,6 +24,7 @@
  *                                                      shapefunc_GS, Get_Stress (eigh, "VM")
  *   fem_bsr_spmv*          SOLVE_static.py:36          KL * U (residual product)
  *   fem_pcg_solve          SOLVE_static.py:31-33       pardisoSolver(KL, mtype=2).factor/solve
+ *   fem_amg_*, fem_pcg_solve_amg  SOLVE_static.py:31-33  the same solve, multigrid-preconditioned
  */
 #ifndef FEM_GB300_H
 #define FEM_GB300_H
@@ -280,6 +283,62 @@ size_t fem_pcg_workspace_bytes(int64_t n_brow, int nrhs, int mixed);
 int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F, double* U,
                   const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
                   void* stream);
+
+/* ---- smoothed-aggregation AMG preconditioner (no reference counterpart) ----------- */
+/* The reference factorises K directly (Pardiso, SOLVE_static.py:31-33).  Block-diagonal
+ * preconditioners stall on slender or stretched meshes (condition numbers of 1e9 and more);
+ * a smoothed-aggregation multigrid V-cycle built on the rigid-body modes does not.
+ * fem_amg is a hierarchy object: fem_amg_setup builds it on the host (HOST arrays: K as FP64
+ * BSR and the node coordinates), fem_amg_upload copies it to the device, fem_amg_destroy
+ * frees it.  Unlike the rest of this interface the object allocates device memory itself
+ * (the FP32 hierarchy, and per-level vectors on first use with a given nrhs).  One host
+ * thread at a time per object. */
+typedef struct fem_amg fem_amg;
+typedef struct fem_amg_opts {
+    double theta;     /* strength of connection: |A_ij|_F > theta sqrt(|A_ii|_F |A_jj|_F)    */
+    int max_levels;   /* levels including the dense coarsest one                             */
+    int max_coarse;   /* the coarsest level is solved densely once it has <= max_coarse DOF */
+    int smooth;       /* 1: Jacobi-smoothed prolongator P = (I - w D^-1 A) T; 0: P = T       */
+    int eig_steps;    /* Lanczos steps estimating lambda_max(D^-1 A) per level              */
+    int pre_degree;   /* Chebyshev pre-smoothing degree (>= 1)                               */
+    int post_degree;  /* Chebyshev post-smoothing degree (>= 1)                              */
+    double cheb_upper; /* smoother interval [upper / cheb_ratio, upper], upper = cheb_upper * lambda_max */
+    double cheb_ratio;
+} fem_amg_opts;
+void fem_amg_default_opts(fem_amg_opts* opts);
+int fem_amg_setup(int64_t n_brow, const int32_t* indptr, const int32_t* indices, const double* vals,
+                  const double* xyz, const fem_amg_opts* opts, fem_amg** out);
+int fem_amg_upload(fem_amg* amg, void* stream);
+void fem_amg_destroy(fem_amg* amg);
+typedef struct fem_amg_level_info {
+    int64_t n;        /* nodes (block rows) of the level                                    */
+    int b;            /* DOF per node (3 on level 0, 6 on coarser levels)                    */
+    int64_t nnzb_A;   /* blocks of the level operator (level 0: 0, the caller's matrix)     */
+    int64_t nnzb_P;   /* blocks of the prolongator (0 on the last level)                     */
+    double lmax;      /* Lanczos estimate of lambda_max(D^-1 A)                              */
+    double omega;     /* prolongator smoothing weight                                        */
+    double setup_s;   /* host seconds spent building this level's transfer and coarse operator */
+} fem_amg_level_info;
+int fem_amg_num_levels(const fem_amg* amg);
+int fem_amg_get_level(const fem_amg* amg, int level, fem_amg_level_info* info);
+/* Host copies of one level's arrays.  what: 0 A (levels >= 1), 1 P, 2 R = P^T, 3 the inverse
+ * diagonal blocks (vals [n][b][b]), 4 the aggregate of each node (indices [n], -1 = none),
+ * 5 the dense inverse of the last level (vals [m][m]).  dims[4] receives (rows, nnzb or
+ * entries, block rows, block cols); call with NULL arrays to size them. */
+int fem_amg_export(const fem_amg* amg, int level, int what, int64_t* dims, int64_t* indptr, int32_t* indices,
+                   double* vals);
+/* One V-cycle z = M^-1 r on the device: FP32 vectors [n][3][nrhs]; A32 the FP32 copy of the
+ * level-0 matrix (FEM_LAYOUT_BSR, _RSOA or _RSOA4). */
+int fem_amg_vcycle(fem_amg* amg, const fem_bsr* A32, int nrhs, const float* r, float* z, void* stream);
+/* fem_pcg_solve with the V-cycle as the preconditioner.  opts->mixed = 1: the cycle
+ * preconditions the FP32 inner solve of the refinement loop.  opts->mixed = 0: FP64 CG with
+ * FP64 products with A64 around the FP32 cycle, with the flexible (Polak-Ribiere) beta; it
+ * converges where FP32 refinement stalls (condition numbers beyond ~1e7).  A32 (the FP32
+ * copy of A64) is required either way; workspace from fem_pcg_workspace_bytes(n, nrhs,
+ * opts->mixed). */
+int fem_pcg_solve_amg(const fem_bsr* A64, const fem_bsr* A32, fem_amg* amg, const double* F, double* U,
+                      const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
+                      void* stream);
 
 /* ---- learned block-Jacobi correction (no reference counterpart) ------------------ */
 /* Per-node MLP 16 -> 64 -> 64 -> 6 (SiLU), BF16 weights in PyTorch [out][in] layout, FP32
