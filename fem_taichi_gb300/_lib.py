@@ -145,7 +145,7 @@ SIGNATURES = {
     "fem_amg_num_levels": (c_int, [c_void_p]),
     "fem_amg_get_level": (c_int, [c_void_p, c_int, ctypes.POINTER(FemAmgLevelInfo)]),
     "fem_amg_export": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
-    "fem_amg_vcycle": (c_int, [c_void_p, ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_void_p]),
+    "fem_amg_vcycle": (c_int, [c_void_p, ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, c_void_p]),
     "fem_pcg_solve_amg": (c_int, [ctypes.POINTER(FemBsr), ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p,
                                   ctypes.POINTER(FemPcgOpts), ctypes.POINTER(FemPcgStats), c_void_p, c_size_t,
                                   c_void_p]),

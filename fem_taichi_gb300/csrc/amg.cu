@@ -261,6 +261,55 @@ __global__ void __launch_bounds__(kThreads) k_cheb0(int64_t n, int R, const floa
     }
 }
 
+// Dirichlet-row update, two steps so that no row reads a value another thread writes:
+// tmp = x_I + D_I^-1 (b - A x)_I for the listed rows, then x_I = tmp.  One thread per (row,
+// right-hand side); the rows are few (the penalised nodes).
+template <typename View>
+__global__ void __launch_bounds__(kThreads) k_dir_fix(const View A, const int32_t* __restrict__ rows, int64_t nrows,
+                                                       int R, const float* __restrict__ b, const float* __restrict__ x,
+                                                       const float* __restrict__ dinv, float* tmp,
+                                                       const PcgState* __restrict__ st) {
+    if (st->done) return;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < nrows * R; t += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t row = rows[t / R];
+        const int k = int(t % R);
+        const int64_t rs = A.indptr[row];
+        const int L = A.indptr[row + 1] - int(rs);
+        float a[3] = {0.f, 0.f, 0.f};
+        for (int l = 0; l < L; ++l) {
+            const int64_t c = A.indices[rs + l];
+            const float* xc = x + 3 * c * R + k;
+            const float x0 = xc[0], x1 = xc[R], x2 = xc[2 * R];
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+                a[p] += *block_value(A, rs, L, l, 3 * p) * x0 + *block_value(A, rs, L, l, 3 * p + 1) * x1 +
+                        *block_value(A, rs, L, l, 3 * p + 2) * x2;
+        }
+        const int64_t o = 3 * row * R + k;
+        const float r0 = b[o] - a[0], r1 = b[o + R] - a[1], r2 = b[o + 2 * R] - a[2];
+        const float* m = dinv + 9 * row;
+        float* tt = tmp + 3 * (t / R) * R + k;
+        tt[0] = x[o] + m[0] * r0 + m[1] * r1 + m[2] * r2;
+        tt[R] = x[o + R] + m[3] * r0 + m[4] * r1 + m[5] * r2;
+        tt[2 * R] = x[o + 2 * R] + m[6] * r0 + m[7] * r1 + m[8] * r2;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_dir_copy(const int32_t* __restrict__ rows, int64_t nrows, int R,
+                                                        const float* __restrict__ tmp, float* x,
+                                                        const PcgState* __restrict__ st) {
+    if (st->done) return;
+    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < nrows * R; t += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t row = rows[t / R];
+        const int k = int(t % R);
+        const int64_t o = 3 * row * R + k;
+        const float* tt = tmp + 3 * (t / R) * R + k;
+        x[o] = tt[0];
+        x[o + R] = tt[R];
+        x[o + 2 * R] = tt[2 * R];
+    }
+}
+
 // dense coarsest solve x = Ainv b: one warp per (row, right-hand side)
 __global__ void __launch_bounds__(kThreads) k_dense(int64_t m, int R, const float* __restrict__ inv,
                                                      const float* __restrict__ b, float* x,
@@ -346,7 +395,8 @@ int cheb_step(fem_amg* h, int l, const View& A0, const float* b, const float* xi
 }
 
 template <typename View>
-int cycle(fem_amg* h, int l, const View& A0, const float* b, float* out, const PcgState* st, int R, cudaStream_t s) {
+int cycle(fem_amg* h, int l, const View& A0, const float* b, float* out, const PcgState* st, int R, bool sym,
+          cudaStream_t s) {
     const int last = int(h->lv.size()) - 1;
     if (l == last) {
         const int64_t work = h->coarse_m * R;
@@ -382,7 +432,7 @@ int cycle(fem_amg* h, int l, const View& A0, const float* b, float* out, const P
     else
         rc = launch_gen<kModes, kModes>(L.dR, L.vr, EpiStore<kModes>{C.vb, R}, st, R, s);
     if (rc) return rc;
-    if ((rc = cycle(h, l + 1, A0, C.vb, C.vo, st, R, s))) return rc;
+    if ((rc = cycle(h, l + 1, A0, C.vb, C.vo, st, R, false, s))) return rc;
     // prolongation
     if (L.b == 3)
         rc = launch_gen<3, kModes>(L.dP, C.vo, EpiAdd<3>{X[cur], R}, st, R, s);
@@ -392,6 +442,12 @@ int cycle(fem_amg* h, int l, const View& A0, const float* b, float* out, const P
     for (int k = 0; k < post; ++k) {
         if ((rc = cheb_step(h, l, A0, b, X[cur], X[cur ^ 1], k == 0 ? 0.f : L.c1[k], L.c2[k], st, R, s))) return rc;
         cur ^= 1;
+    }
+    if (sym && l == 0 && L.n_iso > 0) {
+        const unsigned g = grid_for(L.n_iso * R, kThreads);
+        k_dir_fix<<<g, kThreads, 0, s>>>(A0, L.d_iso_rows, L.n_iso, R, b, out, L.d_dinv, L.vfix, st);
+        k_dir_copy<<<g, kThreads, 0, s>>>(L.d_iso_rows, L.n_iso, R, L.vfix, out, st);
+        FEM_LAUNCH_CHECK("amg Dirichlet rows");
     }
     return FEM_OK;
 }
@@ -431,7 +487,7 @@ void free_bsr(DevBsr& D) {
 
 void free_vectors(fem_amg* h) {
     for (Level& L : h->lv) {
-        for (float** v : {&L.vb, &L.vo, &L.vx, &L.vd, &L.vr}) {
+        for (float** v : {&L.vb, &L.vo, &L.vx, &L.vd, &L.vr, &L.vfix}) {
             cudaFree(*v);
             *v = nullptr;
         }
@@ -452,6 +508,9 @@ void free_device(fem_amg* h) {
         L.d_dinv = nullptr;
         cudaFree(L.d_iso);
         L.d_iso = nullptr;
+        cudaFree(L.d_iso_rows);
+        L.d_iso_rows = nullptr;
+        L.n_iso = 0;
     }
     cudaFree(h->d_coarse_inv);
     h->d_coarse_inv = nullptr;
@@ -477,6 +536,7 @@ int ensure_vectors(fem_amg* h, int R) {
             FEM_CUDA(cudaMalloc(&L.vd, bytes));
             FEM_CUDA(cudaMalloc(&L.vr, bytes));
         }
+        if (L.n_iso > 0) FEM_CUDA(cudaMalloc(&L.vfix, sizeof(float) * size_t(L.n_iso) * L.b * R));
     }
     const size_t b0 = sizeof(float) * size_t(h->lv[0].n) * 3 * R;
     FEM_CUDA(cudaMalloc(&h->r32, b0));
@@ -486,10 +546,11 @@ int ensure_vectors(fem_amg* h, int R) {
 }
 
 template <typename View>
-int vcycle(fem_amg* h, const View& A0, const float* r, float* z, const PcgState* st, int R, cudaStream_t s) {
-    return cycle(h, 0, A0, r, z, st, R, s);
+int vcycle(fem_amg* h, const View& A0, const float* r, float* z, const PcgState* st, int R, bool symmetric,
+           cudaStream_t s) {
+    return cycle(h, 0, A0, r, z, st, R, symmetric, s);
 }
-template int vcycle<BsrView<float>>(fem_amg*, const BsrView<float>&, const float*, float*, const PcgState*, int,
+template int vcycle<BsrView<float>>(fem_amg*, const BsrView<float>&, const float*, float*, const PcgState*, int, bool,
                                      cudaStream_t);
 
 }  // namespace amg
@@ -515,6 +576,13 @@ extern "C" int fem_amg_upload(fem_amg* h, void* stream) {
             rc = upload_array(di, &L.d_dinv);
         }
         if (!rc) rc = upload_array(L.iso, &L.d_iso);
+        if (!rc && l == 0) {
+            std::vector<int32_t> rows;
+            for (size_t i = 0; i < L.iso.size(); ++i)
+                if (L.iso[i]) rows.push_back(int32_t(i));
+            L.n_iso = int64_t(rows.size());
+            rc = upload_array(rows, &L.d_iso_rows);
+        }
     }
     if (!rc) {
         std::vector<float> ci(h->coarse_inv.begin(), h->coarse_inv.end());
@@ -538,7 +606,8 @@ extern "C" void fem_amg_destroy(fem_amg* h) {
     delete h;
 }
 
-extern "C" int fem_amg_vcycle(fem_amg* h, const fem_bsr* A32, int nrhs, const float* r, float* z, void* stream) {
+extern "C" int fem_amg_vcycle(fem_amg* h, const fem_bsr* A32, int nrhs, const float* r, float* z, int symmetric,
+                              void* stream) {
     FEM_REQUIRE(h && A32 && r && z, "NULL argument");
     FEM_REQUIRE(h->uploaded, "call fem_amg_upload first");
     FEM_REQUIRE(A32->dtype == FEM_F32 && A32->n_brow == h->lv[0].n && A32->indptr && A32->indices && A32->vals,
@@ -553,5 +622,5 @@ extern "C" int fem_amg_vcycle(fem_amg* h, const fem_bsr* A32, int nrhs, const fl
     if (rc) return rc;
     const BsrView<float> A{A32->n_brow, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
                            rsoa_kind(A32->layout)};
-    return vcycle(h, A, r, z, static_cast<const pcgd::PcgState*>(h->d_state), nrhs, as_stream(stream));
+    return vcycle(h, A, r, z, static_cast<const pcgd::PcgState*>(h->d_state), nrhs, symmetric != 0, as_stream(stream));
 }

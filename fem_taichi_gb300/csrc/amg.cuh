@@ -55,6 +55,9 @@ struct Level {
     DevBsr dA, dP, dR;
     float* d_dinv = nullptr;
     uint8_t* d_iso = nullptr;
+    int32_t* d_iso_rows = nullptr;  // indices of the Dirichlet rows (level 0)
+    int64_t n_iso = 0;
+    float* vfix = nullptr;          // [n_iso][b][nrhs] scratch of the Dirichlet-row update
     // device vectors for the current nrhs ([n][b][nrhs]): right-hand side and output of this
     // level's cycle (levels >= 1), second iterate, Chebyshev direction, residual
     float *vb = nullptr, *vo = nullptr, *vx = nullptr, *vd = nullptr, *vr = nullptr;
@@ -85,10 +88,15 @@ struct PcgState;
 namespace amg {
 
 // One V-cycle z = M^-1 r on the device for nrhs right-hand sides ([n][3][nrhs] vectors),
-// A0 the level-0 operator in FP32 (the solver's matrix).  Every kernel returns at once when
-// st->done is set, so the sequence can sit inside a captured solver iteration.
+// A0 the level-0 operator in FP32 (the solver's matrix).  symmetric: finish with one
+// block-Jacobi update of the level-0 Dirichlet rows (x_I += D_I^-1 (r - A x)_I), which makes
+// the cycle the symmetric I, F, I product; without it the Dirichlet rows keep
+// x_I = D_I^-1 r_I (no product of a penalty row with a coupled vector, as an FP32 solver
+// needs).  Every kernel returns at once when st->done is set, so the sequence can sit
+// inside a captured solver iteration.
 template <typename View>
-int vcycle(fem_amg* h, const View& A0, const float* r, float* z, const pcgd::PcgState* st, int nrhs, cudaStream_t s);
+int vcycle(fem_amg* h, const View& A0, const float* r, float* z, const pcgd::PcgState* st, int nrhs, bool symmetric,
+           cudaStream_t s);
 
 // Allocates the per-level vectors for nrhs right-hand sides (grow only).
 int ensure_vectors(fem_amg* h, int nrhs);

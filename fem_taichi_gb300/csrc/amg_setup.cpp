@@ -5,23 +5,26 @@
 //
 // Per level (the method of Vanek, Mandel and Brezina, "Algebraic multigrid by smoothed
 // aggregation for second and fourth order elliptic problems", Computing 56 (1996)):
-//  1. strength: j is a strong neighbour of i when |A_ij|_F > theta sqrt(|A_ii|_F |A_jj|_F)
-//     (Frobenius norms of the blocks).  Rows without strong neighbours (above all the
-//     penalised nodes, whose 1e20 diagonal makes every coupling weak) join no aggregate and
-//     are treated as Dirichlet rows: their prolongator rows are zero and the cycle sets
+//  1. strength on the block-scaled matrix: with D_i = L_i L_i^T (Cholesky of the diagonal
+//     block), j is a strong neighbour of i when |L_i^-1 A_ij L_j^-T|_F^2 > theta^2 b (b = DOF
+//     per node, |L_i^-1 A_ii L_i^-T|_F^2 = b), which does not depend on the units of the
+//     DOF.  Rows without strong neighbours join no aggregate.  Among them, rows whose every
+//     scaled coupling is below 1e-6 (the penalised nodes, whose 1e20 diagonal decouples
+//     them) are Dirichlet rows: their prolongator rows are zero and the cycle holds
 //     x_i = D_i^-1 b_i there.  (Coupling them to their neighbours, as a plain smoother or a
 //     smoothed prolongator row would, puts values of size |A_ij x_j| / 1e20 into the
 //     preconditioned vector; multiplied by the penalty again in the next product they cancel
-//     catastrophically in FP32.);
+//     catastrophically in FP32.)  Other unaggregated rows are smoothed like the rest and
+//     keep their smoothed prolongator rows, so the cycle stays symmetric;
 //  2. aggregation, in node order: (a) a free node whose strong neighbours are all free
 //     starts an aggregate with them; (b) every node still free joins the step-(a) aggregate
-//     of its strongest aggregated neighbour; (c) what is left forms aggregates with its free
-//     strong neighbours;
+//     of its most strongly coupled (scaled norm) aggregated neighbour; (c) what is left
+//     forms aggregates with its free strong neighbours;
 //  3. tentative prolongator: per aggregate a QR factorisation (two-pass modified
 //     Gram-Schmidt, numerically dependent columns dropped) of the rows of the near-null
 //     space, B_a = Q_a R_a; T holds Q_a and the next level's near-null space is R_a.  On
 //     level 0 B holds the six rigid-body modes of the node coordinates;
-//  4. P = (I - omega D^-1 A) T on the aggregated rows (zero on the Dirichlet rows),
+//  4. P = (I - omega D^-1 A) T (zero on the Dirichlet rows),
 //     omega = 4 / (3 lambda_max(D^-1 A)), lambda_max from a few Lanczos steps in the D inner
 //     product;
 //  5. A_c = R (A P) with R = P^T, two row-wise sparse products.  Every output row is
@@ -238,24 +241,101 @@ double lanczos_lmax(const HostBsr& A, const std::vector<int64_t>& dpos, const st
     return tridiag_max_eig(alpha, beta);
 }
 
-// Strong-connection flag per block (diagonal blocks are not strong).
-std::vector<uint8_t> strength(const HostBsr& A, const std::vector<double>& dnorm, double theta) {
-    const int bb = A.br * A.bc;
-    std::vector<uint8_t> s(A.nnzb(), 0);
-    const double t2 = theta * theta;
+// Inverse Cholesky factors L_i^-1 (lower triangular) of the diagonal blocks, [n][b][b];
+// a block that is not numerically SPD gets the diagonal scaling 1 / sqrt|d_pp| instead.
+std::vector<double> inv_cholesky(const HostBsr& A, const std::vector<int64_t>& dpos) {
+    const int b = A.br, bb = b * b;
+    std::vector<double> G(size_t(A.n) * bb, 0.0);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < A.n; ++i)
+    for (int64_t i = 0; i < A.n; ++i) {
+        double* g = G.data() + i * bb;
+        if (dpos[i] < 0) {
+            for (int p = 0; p < b; ++p) g[p * b + p] = 1.0;
+            continue;
+        }
+        const double* a = A.val.data() + dpos[i] * bb;
+        double Lm[kModes][kModes] = {};
+        bool ok = true;
+        for (int c = 0; c < b && ok; ++c) {
+            double d = a[c * b + c];
+            for (int k = 0; k < c; ++k) d -= Lm[c][k] * Lm[c][k];
+            if (!(d > 0.0)) {
+                ok = false;
+                break;
+            }
+            Lm[c][c] = sqrt(d);
+            for (int r = c + 1; r < b; ++r) {
+                double v = a[r * b + c];
+                for (int k = 0; k < c; ++k) v -= Lm[r][k] * Lm[c][k];
+                Lm[r][c] = v / Lm[c][c];
+            }
+        }
+        if (!ok) {
+            for (int p = 0; p < b; ++p) {
+                const double d = fabs(a[p * b + p]);
+                g[p * b + p] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+            }
+            continue;
+        }
+        for (int c = 0; c < b; ++c) {  // forward substitution on the unit vectors
+            for (int r = 0; r < b; ++r) {
+                double v = r == c ? 1.0 : 0.0;
+                for (int k = 0; k < r; ++k) v -= Lm[r][k] * g[k * b + c];
+                g[r * b + c] = v / Lm[r][r];
+            }
+        }
+    }
+    return G;
+}
+
+// Strong-connection flag per block (diagonal blocks are not strong), the scaled coupling
+// sv[l] = |L_i^-1 A_ij L_j^-T|_F^2 of every block, and per row the largest sv / b over its
+// off-diagonal blocks.
+std::vector<uint8_t> strength(const HostBsr& A, const std::vector<double>& G, double theta,
+                              std::vector<double>& sv, std::vector<double>& maxc) {
+    const int b = A.br, bb = b * b;
+    std::vector<uint8_t> s(A.nnzb(), 0);
+    sv.assign(A.nnzb(), 0.0);
+    maxc.assign(A.n, 0.0);
+    const double t2 = theta * theta * b;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < A.n; ++i) {
+        const double* gi = G.data() + i * bb;
+        double mx = 0.0;
         for (int64_t l = A.ptr[i]; l < A.ptr[i + 1]; ++l) {
             const int64_t j = A.col[l];
             if (j == i) continue;
-            s[l] = frob2(A.val.data() + l * bb, bb) > t2 * dnorm[i] * dnorm[j] ? 1 : 0;
+            const double* a = A.val.data() + l * bb;
+            const double* gj = G.data() + j * bb;
+            double t[kModes * kModes];  // L_i^-1 A_ij
+            for (int r = 0; r < b; ++r)
+                for (int c = 0; c < b; ++c) {
+                    double v = 0.0;
+                    for (int k = 0; k <= r; ++k) v += gi[r * b + k] * a[k * b + c];
+                    t[r * b + c] = v;
+                }
+            double f = 0.0;  // |(L_i^-1 A_ij) L_j^-T|_F^2
+            for (int r = 0; r < b; ++r)
+                for (int c = 0; c < b; ++c) {
+                    double v = 0.0;
+                    for (int k = 0; k <= c; ++k) v += t[r * b + k] * gj[c * b + k];
+                    f += v * v;
+                }
+            s[l] = f > t2 ? 1 : 0;
+            sv[l] = f;
+            mx = std::max(mx, f / b);
         }
+        maxc[i] = mx;
+    }
     return s;
 }
 
-int64_t aggregate(const HostBsr& A, const std::vector<uint8_t>& strong, std::vector<int32_t>& agg) {
+// Unaggregated rows whose scaled couplings are all below 1e-6 (squared: 1e-12): Dirichlet.
+constexpr double kDecoupled2 = 1e-12;
+
+int64_t aggregate(const HostBsr& A, const std::vector<uint8_t>& strong, const std::vector<double>& sv,
+                  std::vector<int32_t>& agg) {
     const int64_t n = A.n;
-    const int bb = A.br * A.bc;
     constexpr int32_t kFree = -1, kAlone = -2;
     agg.assign(n, kFree);
     for (int64_t i = 0; i < n; ++i) {
@@ -282,7 +362,7 @@ int64_t aggregate(const HostBsr& A, const std::vector<uint8_t>& strong, std::vec
         double bs = -1.0;
         for (int64_t l = A.ptr[i]; l < A.ptr[i + 1]; ++l) {
             if (!strong[l] || first[A.col[l]] < 0) continue;
-            const double s = frob2(A.val.data() + l * bb, bb);
+            const double s = sv[l];
             if (s > bs) {
                 bs = s;
                 best = first[A.col[l]];
@@ -467,10 +547,10 @@ HostBsr transpose(const HostBsr& P) {
     return R;
 }
 
-// P = T - omega D^-1 (A T) (smooth), else P = T; rows of unaggregated nodes stay empty.
+// P = T - omega D^-1 (A T) (smooth), else P = T; rows of Dirichlet nodes stay empty.
 // Row i of A T contains the aggregate of node i itself (A has every diagonal block), so T_i
 // is always added.
-HostBsr drop_rows(const HostBsr& X, const HostBsr& T) {
+HostBsr drop_rows(const HostBsr& X, const std::vector<uint8_t>& drop) {
     HostBsr Y;
     Y.n = X.n;
     Y.m = X.m;
@@ -478,7 +558,7 @@ HostBsr drop_rows(const HostBsr& X, const HostBsr& T) {
     Y.bc = X.bc;
     const int64_t bs = int64_t(X.br) * X.bc;
     Y.ptr.assign(X.n + 1, 0);
-    for (int64_t i = 0; i < X.n; ++i) Y.ptr[i + 1] = Y.ptr[i] + (T.ptr[i + 1] > T.ptr[i] ? X.ptr[i + 1] - X.ptr[i] : 0);
+    for (int64_t i = 0; i < X.n; ++i) Y.ptr[i + 1] = Y.ptr[i] + (drop[i] ? 0 : X.ptr[i + 1] - X.ptr[i]);
     Y.col.resize(Y.ptr[X.n]);
     Y.val.resize(size_t(Y.ptr[X.n]) * bs);
 #pragma omp parallel for schedule(static)
@@ -491,7 +571,7 @@ HostBsr drop_rows(const HostBsr& X, const HostBsr& T) {
 }
 
 HostBsr smooth_prolongator(const HostBsr& A, const std::vector<double>& dinv, const HostBsr& T, double omega,
-                           bool smooth) {
+                           bool smooth, const std::vector<uint8_t>& dirichlet) {
     if (!smooth) return T;
     HostBsr AT = spgemm(A, T);
     const int b = A.br, k = T.bc, bb = b * b, bk = b * k;
@@ -515,7 +595,7 @@ HostBsr smooth_prolongator(const HostBsr& A, const std::vector<double>& dinv, co
             std::copy_n(tmp, bk, blk);
         }
     }
-    return drop_rows(AT, T);
+    return drop_rows(AT, dirichlet);
 }
 
 // Chebyshev coefficients of the smoother on [upper / ratio, upper] for `degree` steps:
@@ -610,10 +690,11 @@ int build(fem_amg* H, HostBsr&& A0, const double* xyz) {
         int64_t na = 0;
         if (!last_by_size) {
             auto ta = Clock::now();
-            const std::vector<uint8_t> strong = strength(A, dnorm, o.theta);
-            na = aggregate(A, strong, L.agg);
+            std::vector<double> sv, maxc;
+            const std::vector<uint8_t> strong = strength(A, inv_cholesky(A, dpos), o.theta, sv, maxc);
+            na = aggregate(A, strong, sv, L.agg);
             L.iso.resize(L.agg.size());
-            for (size_t i = 0; i < L.agg.size(); ++i) L.iso[i] = L.agg[i] < 0 ? 1 : 0;
+            for (size_t i = 0; i < L.agg.size(); ++i) L.iso[i] = (L.agg[i] < 0 && maxc[i] < kDecoupled2) ? 1 : 0;
             H->setup_s[0] += since(ta);
         }
         if (last_by_size || na == 0 || na * kModes >= m) {
@@ -654,7 +735,7 @@ int build(fem_amg* H, HostBsr&& A0, const double* xyz) {
         tentative(A.n, A.br, L.agg, na, B, T, Bc);
         H->setup_s[1] += since(tt);
         auto ts = Clock::now();
-        L.P = smooth_prolongator(A, L.dinv, T, L.omega, o.smooth != 0);
+        L.P = smooth_prolongator(A, L.dinv, T, L.omega, o.smooth != 0, L.iso);
         H->setup_s[3] += since(ts);
         auto tg = Clock::now();
         L.R = transpose(L.P);
@@ -787,6 +868,13 @@ extern "C" int fem_amg_export(const fem_amg* h, int level, int what, int64_t* di
             dims[2] = dims[3] = 1;
             if (indices) std::copy(L.agg.begin(), L.agg.end(), indices);
             return FEM_OK;
+        case 6:
+            dims[0] = L.n;
+            dims[1] = int64_t(L.iso.size());
+            dims[2] = dims[3] = 1;
+            if (indices)
+                for (size_t i = 0; i < L.iso.size(); ++i) indices[i] = L.iso[i];
+            return FEM_OK;
         case 5:
             FEM_REQUIRE(level + 1 == int(h->lv.size()), "the dense inverse belongs to the last level");
             dims[0] = h->coarse_m;
@@ -794,7 +882,7 @@ extern "C" int fem_amg_export(const fem_amg* h, int level, int what, int64_t* di
             dims[2] = dims[3] = 1;
             if (vals) std::copy(h->coarse_inv.begin(), h->coarse_inv.end(), vals);
             return FEM_OK;
-        default: FEM_REQUIRE(false, "what must be 0..5");
+        default: FEM_REQUIRE(false, "what must be 0..6");
     }
     dims[0] = M->n;
     dims[1] = M->nnzb();

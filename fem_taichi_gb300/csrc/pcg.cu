@@ -565,7 +565,7 @@ int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, c
     auto init = [&](cudaStream_t ss) -> int {
         k_init_r<T, R><<<gv, kThreads, 0, ss>>>(nv, b, x, r, r32, part, st, rtol, maxit);
         FEM_LAUNCH_CHECK("k_init_r");
-        int rc = amg::vcycle(amg, A32, rin, zout, st, R, ss);
+        int rc = amg::vcycle(amg, A32, rin, zout, st, R, f64, ss);
         if (rc) return rc;
         k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, nullptr, part, st);
         FEM_LAUNCH_CHECK("k_rz");
@@ -576,7 +576,7 @@ int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, c
             k_p_update<T, R><<<gv, kThreads, 0, ss>>>(nv, z, p, st);
             launch_spmv_pq<T, R>(A, p, q, part, st, variant, ss);
             k_update_r<T, R><<<gv, kThreads, 0, ss>>>(nv, p, q, x, r, r32, part, st);
-            int rc = amg::vcycle(amg, A32, rin, zout, st, R, ss);
+            int rc = amg::vcycle(amg, A32, rin, zout, st, R, f64, ss);
             if (rc) return rc;
             k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, qflex, part, st);
         }

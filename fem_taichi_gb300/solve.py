@@ -99,7 +99,7 @@ class AmgHierarchy:
             _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, ptr.ctypes.data, col.ctypes.data,
                                                val.ctypes.data), "fem_amg_export")
             return ptr, col[:nnz], val[:nnz * br * bc].reshape(nnz, br, bc)
-        if what == 4:
+        if what in (4, 6):
             idx = np.zeros(max(nnz, 1), dtype=np.int32)
             _lib.check(self.lib.fem_amg_export(self.h, level, what, dims, None, idx.ctypes.data, None),
                        "fem_amg_export")

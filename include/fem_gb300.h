@@ -323,13 +323,17 @@ int fem_amg_num_levels(const fem_amg* amg);
 int fem_amg_get_level(const fem_amg* amg, int level, fem_amg_level_info* info);
 /* Host copies of one level's arrays.  what: 0 A (levels >= 1), 1 P, 2 R = P^T, 3 the inverse
  * diagonal blocks (vals [n][b][b]), 4 the aggregate of each node (indices [n], -1 = none),
- * 5 the dense inverse of the last level (vals [m][m]).  dims[4] receives (rows, nnzb or
+ * 5 the dense inverse of the last level (vals [m][m]), 6 the Dirichlet flag of each node
+ * (indices [n]: 1 = decoupled row held at x = D^-1 b in the cycle).  dims[4] receives (rows, nnzb or
  * entries, block rows, block cols); call with NULL arrays to size them. */
 int fem_amg_export(const fem_amg* amg, int level, int what, int64_t* dims, int64_t* indptr, int32_t* indices,
                    double* vals);
 /* One V-cycle z = M^-1 r on the device: FP32 vectors [n][3][nrhs]; A32 the FP32 copy of the
- * level-0 matrix (FEM_LAYOUT_BSR, _RSOA or _RSOA4). */
-int fem_amg_vcycle(fem_amg* amg, const fem_bsr* A32, int nrhs, const float* r, float* z, void* stream);
+ * level-0 matrix (FEM_LAYOUT_BSR, _RSOA or _RSOA4).  symmetric = 1 ends the cycle with one
+ * block-Jacobi update of the Dirichlet rows (the form the FP64 solve uses); 0 holds them at
+ * D^-1 r (the form of the FP32 inner solve, which avoids FP32 products of penalty rows with
+ * coupled vectors). */
+int fem_amg_vcycle(fem_amg* amg, const fem_bsr* A32, int nrhs, const float* r, float* z, int symmetric, void* stream);
 /* fem_pcg_solve with the V-cycle as the preconditioner.  opts->mixed = 1: the cycle
  * preconditions the FP32 inner solve of the refinement loop.  opts->mixed = 0: FP64 CG with
  * FP64 products with A64 around the FP32 cycle, with the flexible (Polak-Ribiere) beta; it

@@ -5,20 +5,22 @@ product's preconditioner (fem_amg_setup / fem_amg_vcycle) follows the published 
 Vanek, Mandel and Brezina (Computing 56, 1996); this module restates the same steps in
 numpy/scipy so the tests can check the library's hierarchy and V-cycle:
 
-* strength: block (i, j), j != i, is strong when |A_ij|_F^2 > theta^2 |A_ii|_F |A_jj|_F;
+* strength on the block-scaled matrix: with D_i = L_i L_i^T, block (i, j), j != i, is strong
+  when |L_i^-1 A_ij L_j^-T|_F^2 > theta^2 b; unaggregated rows whose scaled couplings are all
+  below 1e-6 (|.|_F^2 / b < 1e-12) are Dirichlet rows;
 * aggregation in node order: (a) free node + all-free strong neighbours; (b) join the
-  step-(a) aggregate of the strongest aggregated neighbour; (c) the rest with their free
-  strong neighbours; rows without strong neighbours stay unaggregated;
+  step-(a) aggregate of the most strongly coupled aggregated neighbour; (c) the rest with
+  their free strong neighbours; rows without strong neighbours stay unaggregated;
 * tentative prolongator: two-pass modified Gram-Schmidt of each aggregate's near-null-space
   rows (rigid-body modes on level 0, coordinates taken about the mesh centroid), columns
   whose remaining norm is <= 1e-10 of their original norm dropped;
-* P = T - omega D^-1 A T on the aggregated rows (zero rows for unaggregated nodes) with
+* P = T - omega D^-1 A T (zero rows for Dirichlet nodes) with
   omega = 4 / (3 lambda_max), lambda_max from Lanczos on D^-1 A in the D inner product from
   the same splitmix64 start vector;
 * A_c = P^T A P, zero coarse diagonals set to 1, dense inverse on the last level;
 * V-cycle: Chebyshev pre-smoothing from 0, residual, restriction, coarse cycle,
-  prolongation, Chebyshev post-smoothing restarted from the current iterate; unaggregated
-  (Dirichlet) nodes hold x = D^-1 b throughout and contribute a zero residual.
+  prolongation, Chebyshev post-smoothing restarted from the current iterate; Dirichlet
+  nodes hold x = D^-1 b throughout and contribute a zero residual.
 
 Only ``tests/`` import this module; the product package never does.
 """
@@ -50,20 +52,43 @@ def rigid_modes(xyz):
     return B
 
 
-def strength(A: sp.bsr_matrix, theta):
+def inv_cholesky(A: sp.bsr_matrix):
+    """[n][b][b] inverses of the Cholesky factors of the diagonal blocks (diagonal scaling
+    1 / sqrt|d_pp| where a block is not numerically SPD)."""
     ptr, col, val = _blocks(A)
     n = len(ptr) - 1
+    b = val.shape[1]
+    G = np.zeros((n, b, b))
+    for i in range(n):
+        l = ptr[i] + np.searchsorted(col[ptr[i]:ptr[i + 1]], i)
+        D = val[l]
+        try:
+            Lm = np.linalg.cholesky(D)
+            G[i] = np.linalg.inv(Lm)
+        except np.linalg.LinAlgError:
+            d = np.abs(np.diag(D))
+            G[i] = np.diag(np.where(d > 0, 1.0 / np.sqrt(np.where(d > 0, d, 1.0)), 1.0))
+    return G
+
+
+def strength(A: sp.bsr_matrix, theta):
+    """(ptr, col, scaled squared couplings per block, strong flags, per-row max coupling / b)."""
+    ptr, col, val = _blocks(A)
+    n = len(ptr) - 1
+    b = val.shape[1]
     row = np.repeat(np.arange(n), np.diff(ptr))
-    f2 = (val ** 2).sum(axis=(1, 2))
-    dn = np.zeros(n)
-    diag = row == col
-    dn[row[diag]] = np.sqrt(f2[diag])
-    strong = (row != col) & (f2 > theta * theta * dn[row] * dn[col])
-    return ptr, col, f2, strong
+    G = inv_cholesky(A)
+    S = np.einsum("lrk,lkc,ldc->lrd", G[row], val, G[col])
+    f2 = (S ** 2).sum(axis=(1, 2))
+    off = row != col
+    strong = off & (f2 > theta * theta * b)
+    maxc = np.zeros(n)
+    np.maximum.at(maxc, row[off], f2[off] / b)
+    return ptr, col, f2, strong, maxc
 
 
 def aggregate(A: sp.bsr_matrix, theta):
-    ptr, col, f2, strong = strength(A, theta)
+    ptr, col, f2, strong, maxc = strength(A, theta)
     n = len(ptr) - 1
     FREE, ALONE = -1, -2
     agg = np.full(n, FREE, dtype=np.int64)
@@ -98,7 +123,8 @@ def aggregate(A: sp.bsr_matrix, theta):
                 agg[col[l]] = na
         na += 1
     agg[agg == ALONE] = -1
-    return agg, na
+    dirichlet = (agg < 0) & (maxc < 1e-12)
+    return agg, na, dirichlet
 
 
 def tentative(agg, na, B):
@@ -210,7 +236,7 @@ def setup(K, xyz, theta=0.08, max_levels=10, max_coarse=512, eig_steps=12, lmax_
         levels.append(lv)
         if m <= max_coarse or l + 1 >= max_levels:
             break
-        agg, na = aggregate(A, theta)
+        agg, na, dirichlet = aggregate(A, theta)
         if na == 0 or na * KMODES >= m:
             break
         lm = lanczos_lmax(A, D, Dinv, eig_steps)
@@ -221,7 +247,7 @@ def setup(K, xyz, theta=0.08, max_levels=10, max_coarse=512, eig_steps=12, lmax_
         T, Bc = tentative(agg, na, B)
         Dm = sp.block_diag([sp.csr_matrix(Dinv[i]) for i in range(n)], format="csr")
         P = (T - omega * (Dm @ (sp.csr_matrix(A) @ T))).tocsr()
-        keep = np.repeat(agg >= 0, b).astype(np.float64)
+        keep = np.repeat(~dirichlet, b).astype(np.float64)
         P = (sp.diags(keep) @ P).tocsr()
         P.eliminate_zeros()
         Ac = (P.T @ sp.csr_matrix(A) @ P).tocsr()
@@ -229,7 +255,7 @@ def setup(K, xyz, theta=0.08, max_levels=10, max_coarse=512, eig_steps=12, lmax_
         for d in range(Ac.shape[0]):
             if Ac[d, d] == 0.0:
                 Ac[d, d] = 1.0
-        lv.update(agg=agg, na=na, lmax=lm, omega=omega, P=P)
+        lv.update(agg=agg, na=na, lmax=lm, omega=omega, P=P, dirichlet=dirichlet)
         A = sp.bsr_matrix(Ac.tocsr(), blocksize=(KMODES, KMODES))
         B = Bc
         b = KMODES
@@ -237,15 +263,16 @@ def setup(K, xyz, theta=0.08, max_levels=10, max_coarse=512, eig_steps=12, lmax_
     return levels, coarse
 
 
-def vcycle(levels, coarse_inv, r, pre=2, post=2, upper=1.1, ratio=30.0, l=0):
+def vcycle(levels, coarse_inv, r, pre=2, post=2, upper=1.1, ratio=30.0, l=0, dirichlet_fix=False):
     """FP64 V-cycle z = M^-1 r on the hierarchy (levels[l] needs A, Dinv, b, and for non-last
-    levels P and lmax)."""
+    levels P and lmax).  dirichlet_fix: after the level-0 cycle, one block-Jacobi update on the
+    Dirichlet rows, x_I += D_I^-1 (r - A x)_I (the symmetric I, F, I order)."""
     if l == len(levels) - 1:
         return coarse_inv @ r
     L = levels[l]
     A, b, n = L["A"], L["b"], L["n"]
     Dinv = L["Dinv"]
-    free = np.repeat(L["agg"] >= 0, b)
+    free = np.repeat(~L["dirichlet"], b)
     c1, c2 = chebyshev_coeffs(L["lmax"], max(pre, post), upper, ratio)
     apply_dinv = lambda v: np.einsum("nij,nj->ni", Dinv, v.reshape(n, b)).reshape(-1)  # noqa: E731
     x = np.where(free, c2[0], 1.0) * apply_dinv(r)
@@ -260,4 +287,6 @@ def vcycle(levels, coarse_inv, r, pre=2, post=2, upper=1.1, ratio=30.0, l=0):
         z = apply_dinv(r - A @ x)
         d = c2[k] * z if k == 0 else c1[k] * d + c2[k] * z
         x = np.where(free, x + d, x)
+    if dirichlet_fix and l == 0:
+        x = np.where(free, x, x + apply_dinv(r - A @ x))
     return x

@@ -1,7 +1,7 @@
 """Multigrid hierarchy built by the library on the host (fem_amg_setup, no GPU involved)
 against the numpy restatement in oracle/amg_oracle.py.
 
-Checked per level: the aggregates (bit-exact), the inverse diagonal blocks, the prolongator
+Checked per level: the aggregates and Dirichlet rows (bit-exact), the inverse diagonal blocks, the prolongator
 P, the restriction R = P^T and the coarse operator A_c = P^T A P (all within 1e-12 of the
 largest entry: same arithmetic, different summation order), the Lanczos estimate of
 lambda_max(D^-1 A) (1e-9 relative), and the dense inverse of the last level (1e-10).
@@ -74,6 +74,7 @@ def test_aggregates_prolongator_and_coarse_operator(built):
     P, Kb, H, info, levels, cinv = built
     for l, lv in enumerate(levels[:-1]):
         assert np.array_equal(H.export(l, 4), lv["agg"])
+        assert np.array_equal(H.export(l, 6).astype(bool), lv["dirichlet"])
         b, n, na = lv["b"], lv["n"], lv["na"]
         Pl = bsr_dense(*H.export(l, 1), n * b, na * 6)
         Po = lv["P"].toarray()

@@ -49,6 +49,7 @@ def oracle_levels(S, H):
         lv = {"A": A, "b": b, "n": n, "Dinv": H.export(l, 3).reshape(n, b, b), "lmax": inf["lmax"]}
         if l + 1 < len(info):
             lv["agg"] = H.export(l, 4).astype(np.int64)
+            lv["dirichlet"] = H.export(l, 6).astype(bool)
             ptr, col, blk = H.export(l, 1)
             lv["P"] = sp.bsr_matrix((blk, col, ptr), shape=(n * b, info[l + 1]["n"] * 6)).tocsr()
         levels.append(lv)
@@ -69,8 +70,9 @@ def slab():
     return P, M, S, K, Fv
 
 
+@pytest.mark.parametrize("sym", [0, 1])
 @pytest.mark.parametrize("R", [1, 4])
-def test_vcycle_matches_oracle(slab, R):
+def test_vcycle_matches_oracle(slab, R, sym):
     P, M, S, K, Fv = slab
     H = S.amg(max_coarse=200)
     S.K32()
@@ -80,11 +82,11 @@ def test_vcycle_matches_oracle(slab, R):
     r = rng.standard_normal((3 * P.Num_Node, R)).astype(np.float32)
     rd = torch.from_numpy(r).cuda().contiguous()
     z = torch.full_like(rd, float("nan"))
-    _lib.check(S.lib.fem_amg_vcycle(H.h, S._A32, R, _dptr(rd), _dptr(z), S.stream), "fem_amg_vcycle")
+    _lib.check(S.lib.fem_amg_vcycle(H.h, S._A32, R, _dptr(rd), _dptr(z), sym, S.stream), "fem_amg_vcycle")
     torch.cuda.synchronize()
     z = z.cpu().numpy().astype(np.float64)
     for k in range(R):
-        zo = AO.vcycle(levels, cinv, r[:, k].astype(np.float64))
+        zo = AO.vcycle(levels, cinv, r[:, k].astype(np.float64), dirichlet_fix=bool(sym))
         assert np.linalg.norm(z[:, k] - zo) <= VREL * np.linalg.norm(zo), k
 
 
