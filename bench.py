@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the c3/c4 static-solve studies")
-    ap.add_argument("--c5", action="store_true", help="add the capped 32-RHS twisted-slab study")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 32-RHS twisted-slab (c5) solve study")
     return ap.parse_args()
 
 
@@ -412,8 +412,11 @@ def main():
 
         def brief(r):
             keep = ("label", "wall_s", "iterations", "outer", "relres", "relerr", "meets_1e-8", "status_text",
-                    "ms_per_iteration")
-            return {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
+                    "ms_per_iteration", "nrhs")
+            out = {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
+            if "amg" in r:
+                out["amg_setup"] = r["amg"]
+            return out
 
         r3 = study.c3_study(device=dev, peak_gbs=peak)
         sol = {"c3": brief(r3)}
@@ -422,9 +425,10 @@ def main():
         sol["c4"] = brief(r4)
         sol["c4"]["training"] = r4["training"]
         sol["c4"]["inference_s"] = r4["inference_s"]
-        if a.c5:
-            r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=3000)
+        if not a.no_c5:
+            r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=1000)
             sol["c5"] = brief(r5)
+            sol["c5"]["workload"] = r5["workload"]
         sol["modal_c1"] = study.modal_study("c1", num_eigen=100, num_block=10, device=dev)
         line["solve"] = sol
 
