@@ -178,6 +178,58 @@ __global__ void __launch_bounds__(kThreads) k_bsrgR(const DevView A, const float
     }
 }
 
+// Long rows or few rows: W warps share one block row.  Stream s (of W * 32 / R streams; lane
+// = (stream in warp, right-hand side)) takes blocks s, s + streams, ...; the partial sums are
+// combined by xor shuffles inside each warp and then over the warps through shared memory,
+// in a fixed order.
+template <int BR, int BC, int R, int W, typename Epi>
+__global__ void __launch_bounds__(W * 32) k_bsrg_split(const DevView A, const float* __restrict__ x, const Epi epi,
+                                                        const PcgState* __restrict__ st) {
+    if (st->done) return;
+    constexpr int G = 32 / R;
+    constexpr int S = W * G;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane / R, k = lane % R;
+    const int stream = warp * G + g;
+    __shared__ float red[W][BR][R];
+    for (int64_t row = blockIdx.x; row < A.n; row += gridDim.x) {
+        float acc[BR];
+#pragma unroll
+        for (int r = 0; r < BR; ++r) acc[r] = 0.f;
+        const int e = __ldg(A.ptr + row + 1);
+        for (int l = __ldg(A.ptr + row) + stream; l < e; l += S) {
+            const float* v = A.val + int64_t(l) * (BR * BC);
+            const float* xc = x + int64_t(__ldg(A.col + l)) * BC * R + k;
+            float xs[BC];
+#pragma unroll
+            for (int q = 0; q < BC; ++q) xs[q] = xc[q * R];
+#pragma unroll
+            for (int r = 0; r < BR; ++r)
+#pragma unroll
+                for (int q = 0; q < BC; ++q) acc[r] += __ldg(v + r * BC + q) * xs[q];
+        }
+#pragma unroll
+        for (int off = R; off < 32; off <<= 1)
+#pragma unroll
+            for (int r = 0; r < BR; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], off);
+        if (g == 0) {
+#pragma unroll
+            for (int r = 0; r < BR; ++r) red[warp][r][k] = acc[r];
+        }
+        __syncthreads();
+        if (warp == 0 && g == 0) {
+            float tot[BR];
+#pragma unroll
+            for (int r = 0; r < BR; ++r) {
+                tot[r] = red[0][r][k];
+                for (int w = 1; w < W; ++w) tot[r] += red[w][r][k];
+            }
+            epi(row, k, tot);
+        }
+        __syncthreads();
+    }
+}
+
 // ---- level-0 epilogues (spmv.cuh interface: o = first component, stride = R) ----------------
 struct Epi0Resid {
     const float* b;
@@ -262,21 +314,24 @@ __global__ void __launch_bounds__(kThreads) k_cheb0(int64_t n, int R, const floa
 }
 
 // Dirichlet-row update, two steps so that no row reads a value another thread writes:
-// tmp = x_I + D_I^-1 (b - A x)_I for the listed rows, then x_I = tmp.  One thread per (row,
-// right-hand side); the rows are few (the penalised nodes).
+// tmp = x_I + D_I^-1 (b - A x)_I for the listed rows, then x_I = tmp.  One warp per (row,
+// right-hand side), lanes over the row's blocks; the rows are few (the penalised nodes).
 template <typename View>
 __global__ void __launch_bounds__(kThreads) k_dir_fix(const View A, const int32_t* __restrict__ rows, int64_t nrows,
                                                        int R, const float* __restrict__ b, const float* __restrict__ x,
                                                        const float* __restrict__ dinv, float* tmp,
                                                        const PcgState* __restrict__ st) {
     if (st->done) return;
-    for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < nrows * R; t += int64_t(gridDim.x) * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t t = warp; t < nrows * R; t += nwarps) {
         const int64_t row = rows[t / R];
         const int k = int(t % R);
         const int64_t rs = A.indptr[row];
         const int L = A.indptr[row + 1] - int(rs);
         float a[3] = {0.f, 0.f, 0.f};
-        for (int l = 0; l < L; ++l) {
+        for (int l = lane; l < L; l += 32) {
             const int64_t c = A.indices[rs + l];
             const float* xc = x + 3 * c * R + k;
             const float x0 = xc[0], x1 = xc[R], x2 = xc[2 * R];
@@ -285,13 +340,17 @@ __global__ void __launch_bounds__(kThreads) k_dir_fix(const View A, const int32_
                 a[p] += *block_value(A, rs, L, l, 3 * p) * x0 + *block_value(A, rs, L, l, 3 * p + 1) * x1 +
                         *block_value(A, rs, L, l, 3 * p + 2) * x2;
         }
-        const int64_t o = 3 * row * R + k;
-        const float r0 = b[o] - a[0], r1 = b[o + R] - a[1], r2 = b[o + 2 * R] - a[2];
-        const float* m = dinv + 9 * row;
-        float* tt = tmp + 3 * (t / R) * R + k;
-        tt[0] = x[o] + m[0] * r0 + m[1] * r1 + m[2] * r2;
-        tt[R] = x[o + R] + m[3] * r0 + m[4] * r1 + m[5] * r2;
-        tt[2 * R] = x[o + 2 * R] + m[6] * r0 + m[7] * r1 + m[8] * r2;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) a[p] = group_sum<32>(a[p]);
+        if (lane == 0) {
+            const int64_t o = 3 * row * R + k;
+            const float r0 = b[o] - a[0], r1 = b[o + R] - a[1], r2 = b[o + 2 * R] - a[2];
+            const float* m = dinv + 9 * row;
+            float* tt = tmp + 3 * (t / R) * R + k;
+            tt[0] = x[o] + m[0] * r0 + m[1] * r1 + m[2] * r2;
+            tt[R] = x[o + R] + m[3] * r0 + m[4] * r1 + m[5] * r2;
+            tt[2 * R] = x[o + 2 * R] + m[6] * r0 + m[7] * r1 + m[8] * r2;
+        }
     }
 }
 
@@ -338,10 +397,40 @@ int lanes_for(const DevBsr& M) {
     return avg < 6 ? 4 : avg < 16 ? 8 : avg < 48 ? 16 : 32;
 }
 
-// y (op) = M x for the generic levels; dispatch on block shape and nrhs
+template <int BR, int BC, int R, typename Epi>
+void launch_split(const DevView& v, double avg, const float* x, const Epi& epi, const PcgState* st, cudaStream_t s) {
+    // about four blocks per stream: W * (32 / R) streams ~ avg / 4 (R > 1), ~ avg / 2 (R == 1)
+    constexpr int G = 32 / R;
+    const double want = (R == 1 ? avg / 2.0 : avg / 4.0) / G;
+    const int W = want > 4 ? 8 : want > 2 ? 4 : want > 1 ? 2 : 1;
+    const int64_t cap = int64_t(sm_count()) * (2048 / (W * 32)) * 4;
+    const unsigned g = unsigned(std::max<int64_t>(1, std::min<int64_t>(v.n, cap)));
+    switch (W) {
+        case 8: k_bsrg_split<BR, BC, R, 8><<<g, 256, 0, s>>>(v, x, epi, st); break;
+        case 4: k_bsrg_split<BR, BC, R, 4><<<g, 128, 0, s>>>(v, x, epi, st); break;
+        case 2: k_bsrg_split<BR, BC, R, 2><<<g, 64, 0, s>>>(v, x, epi, st); break;
+        default: k_bsrg_split<BR, BC, R, 1><<<g, 32, 0, s>>>(v, x, epi, st); break;
+    }
+}
+
+// y (op) = M x for the generic levels; dispatch on block shape, nrhs and row length: many
+// short rows take several rows per warp, long rows the split-row kernel
 template <int BR, int BC, typename Epi>
 int launch_gen(const DevBsr& M, const float* x, const Epi& epi, const PcgState* st, int R, cudaStream_t s) {
     const DevView v = view(M);
+    const double avg = M.n > 0 ? double(M.nnzb) / double(M.n) : 1.0;
+    if (avg >= (R == 1 ? 24.0 : 8.0)) {
+        switch (R) {
+            case 1: launch_split<BR, BC, 1>(v, avg, x, epi, st, s); break;
+            case 2: launch_split<BR, BC, 2>(v, avg, x, epi, st, s); break;
+            case 4: launch_split<BR, BC, 4>(v, avg, x, epi, st, s); break;
+            case 8: launch_split<BR, BC, 8>(v, avg, x, epi, st, s); break;
+            case 16: launch_split<BR, BC, 16>(v, avg, x, epi, st, s); break;
+            default: launch_split<BR, BC, 32>(v, avg, x, epi, st, s); break;
+        }
+        FEM_LAUNCH_CHECK("amg block-row product (split rows)");
+        return FEM_OK;
+    }
     if (R == 1) {
         const int lpr = lanes_for(M);
         const unsigned g = grid_for(M.n, (kThreads / 32) * (32 / lpr));
@@ -444,9 +533,9 @@ int cycle(fem_amg* h, int l, const View& A0, const float* b, float* out, const P
         cur ^= 1;
     }
     if (sym && l == 0 && L.n_iso > 0) {
-        const unsigned g = grid_for(L.n_iso * R, kThreads);
-        k_dir_fix<<<g, kThreads, 0, s>>>(A0, L.d_iso_rows, L.n_iso, R, b, out, L.d_dinv, L.vfix, st);
-        k_dir_copy<<<g, kThreads, 0, s>>>(L.d_iso_rows, L.n_iso, R, L.vfix, out, st);
+        k_dir_fix<<<grid_for(L.n_iso * R, kThreads / 32), kThreads, 0, s>>>(A0, L.d_iso_rows, L.n_iso, R, b, out,
+                                                                             L.d_dinv, L.vfix, st);
+        k_dir_copy<<<grid_for(L.n_iso * R, kThreads), kThreads, 0, s>>>(L.d_iso_rows, L.n_iso, R, L.vfix, out, st);
         FEM_LAUNCH_CHECK("amg Dirichlet rows");
     }
     return FEM_OK;
