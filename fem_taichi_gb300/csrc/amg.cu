@@ -31,13 +31,28 @@ namespace {
 using pcgd::PcgState;
 constexpr int kThreads = 256;
 
+// Device matrices are kept twice: row-SoA (val: the values of block row i, L blocks from
+// ptr[i], at val[BB * ptr[i] + q * L + l] for value q of slot l, so lanes that take
+// consecutive slots read consecutive words; used with one right-hand side) and block-major
+// (valb[BB * (ptr[i] + l) + q]: a block in one or two cache lines, for the many-RHS kernels
+// whose lanes of a row all read the same block).
 struct DevView {
     int64_t n;
     const int32_t* ptr;
     const int32_t* col;
     const float* val;
+    const float* valb;
 };
-inline DevView view(const DevBsr& M) { return DevView{M.n, M.ptr, M.col, M.val}; }
+inline DevView view(const DevBsr& M) { return DevView{M.n, M.ptr, M.col, M.val, M.valb}; }
+
+// value (r, q) of slot li of a row starting at block rs with L blocks
+template <int BR, int BC, bool SOA>
+__device__ __forceinline__ float blk(const DevView& A, int rs, int L, int li, int r, int q) {
+    if constexpr (SOA)
+        return __ldg(A.val + int64_t(rs) * (BR * BC) + int64_t(r * BC + q) * L + li);
+    else
+        return __ldg(A.valb + (int64_t(rs) + li) * (BR * BC) + r * BC + q);
+}
 
 // ---- epilogues of the generic block-row product (row, right-hand side k, BR row sums) ----
 template <int BR>
@@ -127,17 +142,17 @@ __global__ void __launch_bounds__(kThreads) k_bsrg1(const DevView A, const float
 #pragma unroll
         for (int r = 0; r < BR; ++r) acc[r] = 0.f;
         if (valid) {
-            const int e = __ldg(A.ptr + row + 1);
-            for (int l = __ldg(A.ptr + row) + sl; l < e; l += LPR) {
-                const float* v = A.val + int64_t(l) * (BR * BC);
-                const float* xc = x + int64_t(__ldg(A.col + l)) * BC;
+            const int rs = __ldg(A.ptr + row);
+            const int L = __ldg(A.ptr + row + 1) - rs;
+            for (int li = sl; li < L; li += LPR) {
+                const float* xc = x + int64_t(__ldg(A.col + rs + li)) * BC;
                 float xs[BC];
 #pragma unroll
                 for (int q = 0; q < BC; ++q) xs[q] = xc[q];
 #pragma unroll
                 for (int r = 0; r < BR; ++r)
 #pragma unroll
-                    for (int q = 0; q < BC; ++q) acc[r] += __ldg(v + r * BC + q) * xs[q];
+                    for (int q = 0; q < BC; ++q) acc[r] += blk<BR, BC, true>(A, rs, L, li, r, q) * xs[q];
             }
         }
 #pragma unroll
@@ -162,17 +177,17 @@ __global__ void __launch_bounds__(kThreads) k_bsrgR(const DevView A, const float
         float acc[BR];
 #pragma unroll
         for (int r = 0; r < BR; ++r) acc[r] = 0.f;
-        const int e = __ldg(A.ptr + row + 1);
-        for (int l = __ldg(A.ptr + row); l < e; ++l) {
-            const float* v = A.val + int64_t(l) * (BR * BC);
-            const float* xc = x + int64_t(__ldg(A.col + l)) * BC * R + k;
+        const int rs = __ldg(A.ptr + row);
+        const int L = __ldg(A.ptr + row + 1) - rs;
+        for (int li = 0; li < L; ++li) {
+            const float* xc = x + int64_t(__ldg(A.col + rs + li)) * BC * R + k;
             float xs[BC];
 #pragma unroll
             for (int q = 0; q < BC; ++q) xs[q] = xc[q * R];
 #pragma unroll
             for (int r = 0; r < BR; ++r)
 #pragma unroll
-                for (int q = 0; q < BC; ++q) acc[r] += __ldg(v + r * BC + q) * xs[q];
+                for (int q = 0; q < BC; ++q) acc[r] += blk<BR, BC, false>(A, rs, L, li, r, q) * xs[q];
         }
         epi(row, k, acc);
     }
@@ -196,17 +211,17 @@ __global__ void __launch_bounds__(W * 32) k_bsrg_split(const DevView A, const fl
         float acc[BR];
 #pragma unroll
         for (int r = 0; r < BR; ++r) acc[r] = 0.f;
-        const int e = __ldg(A.ptr + row + 1);
-        for (int l = __ldg(A.ptr + row) + stream; l < e; l += S) {
-            const float* v = A.val + int64_t(l) * (BR * BC);
-            const float* xc = x + int64_t(__ldg(A.col + l)) * BC * R + k;
+        const int rs = __ldg(A.ptr + row);
+        const int L = __ldg(A.ptr + row + 1) - rs;
+        for (int li = stream; li < L; li += S) {
+            const float* xc = x + int64_t(__ldg(A.col + rs + li)) * BC * R + k;
             float xs[BC];
 #pragma unroll
             for (int q = 0; q < BC; ++q) xs[q] = xc[q * R];
 #pragma unroll
             for (int r = 0; r < BR; ++r)
 #pragma unroll
-                for (int q = 0; q < BC; ++q) acc[r] += __ldg(v + r * BC + q) * xs[q];
+                for (int q = 0; q < BC; ++q) acc[r] += blk<BR, BC, R == 1>(A, rs, L, li, r, q) * xs[q];
         }
 #pragma unroll
         for (int off = R; off < 32; off <<= 1)
@@ -549,6 +564,7 @@ int upload_array(const std::vector<T>& h, T** d) {
     return FEM_OK;
 }
 
+// FP32 row-SoA and block-major copies (see DevView) with 32-bit row pointers.
 int upload_bsr(const HostBsr& H, DevBsr& D) {
     D.n = H.n;
     D.m = H.m;
@@ -558,20 +574,31 @@ int upload_bsr(const HostBsr& H, DevBsr& D) {
     if (H.ptr.empty()) return FEM_OK;
     FEM_REQUIRE(H.nnzb() < (int64_t(1) << 31), "AMG matrix too large for 32-bit row pointers");
     std::vector<int32_t> p(H.ptr.begin(), H.ptr.end());
-    std::vector<float> v(H.val.begin(), H.val.end());
+    const int64_t bb = int64_t(H.br) * H.bc;
+    std::vector<float> v(H.val.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < H.n; ++i) {
+        const int64_t rs = H.ptr[i], L = H.ptr[i + 1] - rs;
+        for (int64_t l = 0; l < L; ++l)
+            for (int64_t q = 0; q < bb; ++q) v[bb * rs + q * L + l] = float(H.val[(rs + l) * bb + q]);
+    }
     int rc;
     if ((rc = upload_array(p, &D.ptr))) return rc;
     if ((rc = upload_array(H.col, &D.col))) return rc;
-    return upload_array(v, &D.val);
+    if ((rc = upload_array(v, &D.val))) return rc;
+    std::vector<float> vb(H.val.begin(), H.val.end());
+    return upload_array(vb, &D.valb);
 }
 
 void free_bsr(DevBsr& D) {
     cudaFree(D.ptr);
     cudaFree(D.col);
     cudaFree(D.val);
+    cudaFree(D.valb);
     D.ptr = nullptr;
     D.col = nullptr;
     D.val = nullptr;
+    D.valb = nullptr;
 }
 
 void free_vectors(fem_amg* h) {

@@ -28,14 +28,15 @@ struct HostBsr {
     int64_t nnzb() const { return ptr.empty() ? 0 : ptr.back(); }
 };
 
-// Device BSR matrix, FP32, 32-bit row pointers.
+// Device BSR matrix, FP32, 32-bit row pointers, values in two layouts (amg.cu).
 struct DevBsr {
     int64_t n = 0, m = 0;
     int br = 0, bc = 0;
     int64_t nnzb = 0;
     int32_t* ptr = nullptr;
     int32_t* col = nullptr;
-    float* val = nullptr;
+    float* val = nullptr;   // row-SoA values
+    float* valb = nullptr;  // block-major values
 };
 
 struct Level {
