@@ -9,8 +9,8 @@ sqrt(lambda) / 2 pi.
 Here every vector lives in HBM: M is applied as a BSR SpMM (the scalar-per-block mass matrix
 expanded to diagonal 3x3 blocks), each K^-1 M u is one multi-right-hand-side PCG solve of the
 whole block (FP32 inner solves inside FP64 refinement, ``fem_pcg_solve`` with the block padded
-to the next supported count), and the reorthogonalisation products are FP64 GEMMs on the
-device.  Only the (2 num_eigen)^2 projection T is diagonalised on the host.
+to the next supported count; preconditioned by the multigrid V-cycle by default, or block
+Jacobi), and the reorthogonalisation products are FP64 GEMMs on the device.  Only the (2 num_eigen)^2 projection T is diagonalised on the host.
 
 ``Eigen_solver(Model).Solve_cpu(num_eigen, num_block)`` keeps the reference's signature and
 returns (freq (num_eigen,), vectors (3N, num_eigen)); it runs the GPU path (there is no CPU
@@ -72,9 +72,13 @@ class Eigen_solver:
         _lib.check(S.lib.fem_bsr_spmv(ctypes.byref(A), R, _dptr(Xp), _dptr(Y), 0, S.stream), "fem_bsr_spmv (M)")
         return Y[:, :b]
 
-    def Solve_gpu(self, num_eigen=100, num_block=10, rtol=1e-11, seed=0, u0=None, mixed=True):
+    def Solve_gpu(self, num_eigen=100, num_block=10, rtol=1e-11, seed=0, u0=None, mixed=True, precond="amg"):
         """Block Lanczos (SOLVE_eigen.py:45-89) on the device.  Returns (lambda (num_eigen,),
-        vectors (3N, num_eigen)) as device tensors, lambda ascending."""
+        vectors (3N, num_eigen)) as device tensors, lambda ascending.  precond: "amg"
+        (multigrid V-cycle, built once per solver) or "bj" (block Jacobi) for the K solves."""
+        if precond not in ("amg", "bj"):
+            raise ValueError("precond must be 'amg' or 'bj'")
+        pc = "amg" if precond == "amg" else None
         if self.Qtype != 0:
             raise NotImplementedError("only the linear modal problem (Qtype 0) is built")
         S = self._system()
@@ -95,7 +99,7 @@ class Eigen_solver:
         Q[:, :b] = u
         iters = 0
         for i in range(steps):
-            w, st = S.solve(F=self._apply_M(u), rtol=rtol, mixed=mixed)
+            w, st = S.solve(F=self._apply_M(u), rtol=rtol, mixed=mixed, precond=pc)
             if st["status"] != 0:
                 raise _lib.FemError(st["status"], f"K solve of Lanczos step {i}: {st['status_text']}")
             iters += st["iterations"]

@@ -300,22 +300,23 @@ def solve_probe(cfg="c3", iterations=40, device="cuda", variant64=None, variant3
     return out
 
 
-def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda"):
+def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda", precond="amg"):
     """Block-Lanczos modal solve (SOLVE_eigen.py:45-89, the reference driver's num_eigen=100)
     on a config mesh: wall time of a warm solve and the lowest frequencies."""
     from .eigen import Eigen_solver
     P = _mesh.config_mesh(cfg)
     M = Model(cfg, P, STEEL, device=device)
     solver = Eigen_solver(M)
-    solver.Solve_gpu(num_eigen=min(num_eigen, 10), num_block=min(num_block, 5))  # warm: FP32 copy, graphs
+    solver.Solve_gpu(num_eigen=min(num_eigen, 10), num_block=min(num_block, 5), precond=precond)  # warm
     torch.cuda.synchronize()
     t = time.perf_counter()
-    lam, X = solver.Solve_gpu(num_eigen=num_eigen, num_block=num_block)
+    lam, X = solver.Solve_gpu(num_eigen=num_eigen, num_block=num_block, precond=precond)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t
     freq = (torch.sqrt(lam) / 2 / np.pi).cpu().numpy()
     G = X.T @ solver._apply_M(X)
     orth = float((G - torch.eye(num_eigen, dtype=G.dtype, device=G.device)).abs().max())
-    return {"workload": f"{cfg}: {P.Num_Node:,} nodes, {num_eigen} modes, block {num_block}", "wall_s": wall,
+    return {"workload": f"{cfg}: {P.Num_Node:,} nodes, {num_eigen} modes, block {num_block}", "precond": precond,
+            "wall_s": wall,
             "steps": solver.last_stats["steps"], "solve_iterations": solver.last_stats["solve_iterations"],
             "lowest_freq_hz": [float(f) for f in freq[:5]], "M_orthonormality_err": orth}

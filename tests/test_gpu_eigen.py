@@ -21,7 +21,8 @@ def _model(nx=8, ny=5, nz=4, seed=3):
     return F.Model("e", P, STEEL)
 
 
-def test_lanczos_matches_oracle_same_start_block():
+@pytest.mark.parametrize("precond", ["amg", "bj"])
+def test_lanczos_matches_oracle_same_start_block(precond):
     M = _model()
     K, Mm = M.Get_MatrixKL().tocsc(), M.Get_MatrixM().tocsr()
     n = K.shape[0]
@@ -30,7 +31,7 @@ def test_lanczos_matches_oracle_same_start_block():
     lu = spla.splu(K)
     lam_o, X_o = EO.lanczos(lu.solve, Mm, u0, ne, nb)
     solver = F.Eigen_solver(M)
-    lam, X = solver.Solve_gpu(num_eigen=ne, num_block=nb, u0=u0)
+    lam, X = solver.Solve_gpu(num_eigen=ne, num_block=nb, u0=u0, precond=precond)
     lam, X = lam.cpu().numpy(), X.cpu().numpy()
     assert np.all(np.abs(lam - lam_o) <= 1e-8 * np.abs(lam_o))
     G = X.T @ (Mm @ X)
