@@ -363,8 +363,17 @@ class Static_solver:
 
     def Solve_cpu(self, max_errs=1e-4, max_iters=20):
         """SOLVE_static.py:12-75 signature: returns U (3N,).  Qtype 0 runs the GPU linear solve
-        to a relative residual of 1e-12 (the reference used a direct factorisation); Qtype 1
-        the large-displacement Newton iteration (Solve_nonlinear)."""
+        to a relative residual of 1e-12 (the reference used a direct factorisation, which
+        always returns a solution): mixed block-Jacobi PCG first (capped at 20,000
+        iterations), and when that does not converge (slender or stretched meshes) the FP64
+        multigrid solve to 1e-10, whose residual is near the FP64 floor of such systems;
+        ``last_stats["fallback_from"]`` then holds the first attempt.  Qtype 1 runs the
+        large-displacement Newton iteration (Solve_nonlinear)."""
         if self.Qtype == 1:
             return self.Solve_nonlinear(max_errs=max_errs, max_iters=max_iters)
-        return self.Solve_gpu(rtol=1e-12, mixed=True)
+        U = self.Solve_gpu(rtol=1e-12, mixed=True, maxit=20000)
+        if self.last_stats["status"] != 0:
+            first = self.last_stats
+            U = self.Solve_gpu(rtol=1e-10, mixed=False, precond="amg")
+            self.last_stats["fallback_from"] = first
+        return U

@@ -144,3 +144,18 @@ def test_amg_solve_c1_against_direct():
         assert "fallback_from" not in st
         assert relerr(U.cpu().numpy(), Ur) <= ERR, st
         assert st["iterations"] < 200, st
+
+
+def test_drop_in_solve_falls_back_to_multigrid_on_the_slab(slab):
+    """Static_solver(Model).Solve_cpu (the reference's entry point): block Jacobi does not
+    converge on the slender slab within its cap, so the multigrid FP64 solve takes over and
+    the answer matches SuperLU."""
+    P, M, S, K, Fv = slab
+    Ur = spla.splu(K.tocsc()).solve(Fv)
+    solver = F.Static_solver(M)
+    U = solver.Solve_cpu()
+    st = solver.last_stats
+    assert relerr(U, Ur) <= ERR, st
+    assert st["status"] == 0
+    if "fallback_from" in st:
+        assert st["precond"] == "amg" and st["fallback_from"]["status"] != 0
