@@ -182,3 +182,52 @@ def test_bad_inputs_refused():
     rc = L.fem_amg_setup(2, ip.ctypes.data, ix.ctypes.data, va.ctypes.data, xy.ctypes.data, ctypes.byref(o),
                          ctypes.byref(h))
     assert rc == _lib.FEM_ERR_INVALID
+
+
+def _setup(Kb, xyz, **opts):
+    return AmgHierarchy(_lib.load(), Kb.shape[0] // 3, Kb.indptr, Kb.indices, Kb.data, xyz, None, **opts)
+
+
+def test_single_dense_level_when_small():
+    """A system at most max_coarse DOF is one dense level: its inverse is K^-1."""
+    P = F.hex_block(3, 2, 2, jitter=0.1, seed=9, fix="zmin")
+    Kb = host_system(P)
+    H = _setup(Kb, P.xyz, max_coarse=10000)
+    assert len(H.levels()) == 1
+    inv = H.export(0, 5).reshape(Kb.shape)
+    Kd = Kb.toarray()
+    assert np.abs(inv @ Kd - np.eye(Kd.shape[0])).max() <= 1e-8
+
+
+def test_all_penalised_nodes_give_no_aggregates():
+    """Every diagonal entry penalised (1e20): no strong couplings, no aggregates, all rows
+    Dirichlet on the dense level; the setup still succeeds."""
+    P = F.hex_block(4, 3, 3, jitter=0.1, seed=2, fix=None)
+    Kb = host_system(P)
+    Kb = sp.bsr_matrix(Kb.tocsr() + sp.identity(Kb.shape[0]) * 1e20, blocksize=(3, 3))
+    Kb.sort_indices()
+    H = _setup(Kb, P.xyz, max_coarse=10)
+    lv = H.levels()
+    assert len(lv) == 1 and lv[0]["n"] == P.Num_Node
+
+
+def test_theta_zero_and_one_level_cap():
+    P = F.hex_block(6, 4, 3, jitter=0.1, seed=4, fix="xmin")
+    Kb = host_system(P)
+    H = _setup(Kb, P.xyz, theta=0.0, max_coarse=60)
+    lv = H.levels()
+    assert len(lv) >= 2 and lv[1]["n"] < lv[0]["n"]
+    H1 = _setup(Kb, P.xyz, max_levels=1)
+    assert len(H1.levels()) == 1
+
+
+def test_uncoarsenable_large_level_is_refused():
+    """A level that is too large for the dense solve and cannot be coarsened (a purely
+    diagonal system: no couplings) is refused with FEM_ERR_INVALID, not run."""
+    n = 3000
+    Kb = sp.bsr_matrix(sp.identity(3 * n, format="csr") * 2.0, blocksize=(3, 3))
+    Kb.sort_indices()
+    xyz = np.random.default_rng(0).uniform(size=(n, 3))
+    with pytest.raises(_lib.FemError) as e:
+        _setup(Kb, xyz, max_coarse=100)
+    assert e.value.code == _lib.FEM_ERR_INVALID
