@@ -143,6 +143,7 @@ SIGNATURES = {
     "fem_amg_upload": (c_int, [c_void_p, c_void_p]),
     "fem_amg_destroy": (None, [c_void_p]),
     "fem_amg_num_levels": (c_int, [c_void_p]),
+    "fem_amg_setup_phases": (c_int, [c_void_p, c_void_p]),
     "fem_amg_get_level": (c_int, [c_void_p, c_int, ctypes.POINTER(FemAmgLevelInfo)]),
     "fem_amg_export": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fem_amg_vcycle": (c_int, [c_void_p, ctypes.POINTER(FemBsr), c_int, c_void_p, c_void_p, c_int, c_void_p]),

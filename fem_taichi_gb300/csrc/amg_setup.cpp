@@ -449,24 +449,24 @@ void tentative(int64_t n, int b, const std::vector<int32_t>& agg, int64_t na, co
     }
 }
 
-// z (bi x bj) += x (bi x bk) y (bk x bj)
-inline void block_fma(int bi, int bk, int bj, const double* x, const double* y, double* z) {
-    for (int r = 0; r < bi; ++r)
-        for (int q = 0; q < bk; ++q) {
-            const double xv = x[r * bk + q];
-            if (xv == 0.0) continue;
-            for (int c = 0; c < bj; ++c) z[r * bj + c] += xv * y[q * bj + c];
+// z (BI x BJ) += x (BI x BK) y (BK x BJ); block shapes fixed at compile time
+template <int BI, int BK, int BJ>
+inline void block_fma(const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ z) {
+    for (int r = 0; r < BI; ++r)
+        for (int q = 0; q < BK; ++q) {
+            const double xv = x[r * BK + q];
+            for (int c = 0; c < BJ; ++c) z[r * BJ + c] += xv * y[q * BJ + c];
         }
 }
 
 // Z = X Y, row by row (Gustavson); columns ascending in every output row.
-HostBsr spgemm(const HostBsr& X, const HostBsr& Y) {
+template <int BI, int BK, int BJ>
+HostBsr spgemm_t(const HostBsr& X, const HostBsr& Y) {
     HostBsr Z;
     Z.n = X.n;
     Z.m = Y.m;
-    Z.br = X.br;
-    Z.bc = Y.bc;
-    const int bi = X.br, bk = X.bc, bj = Y.bc;
+    Z.br = BI;
+    Z.bc = BJ;
     Z.ptr.assign(Z.n + 1, 0);
 #pragma omp parallel
     {
@@ -487,7 +487,7 @@ HostBsr spgemm(const HostBsr& X, const HostBsr& Y) {
     }
     for (int64_t i = 0; i < Z.n; ++i) Z.ptr[i + 1] += Z.ptr[i];
     Z.col.assign(Z.ptr[Z.n], 0);
-    Z.val.assign(size_t(Z.ptr[Z.n]) * bi * bj, 0.0);
+    Z.val.assign(size_t(Z.ptr[Z.n]) * BI * BJ, 0.0);
 #pragma omp parallel
     {
         std::vector<int32_t> pos(Y.m, -1);
@@ -509,12 +509,12 @@ HostBsr spgemm(const HostBsr& X, const HostBsr& Y) {
                 pos[list[q]] = int32_t(q);
                 Z.col[base + q] = list[q];
             }
+            double* zr = Z.val.data() + base * BI * BJ;
             for (int64_t l = X.ptr[i]; l < X.ptr[i + 1]; ++l) {
                 const int64_t kk = X.col[l];
-                const double* xb = X.val.data() + l * bi * bk;
+                const double* xb = X.val.data() + l * BI * BK;
                 for (int64_t t = Y.ptr[kk]; t < Y.ptr[kk + 1]; ++t)
-                    block_fma(bi, bk, bj, xb, Y.val.data() + t * bk * bj,
-                              Z.val.data() + (base + pos[Y.col[t]]) * bi * bj);
+                    block_fma<BI, BK, BJ>(xb, Y.val.data() + t * BK * BJ, zr + int64_t(pos[Y.col[t]]) * BI * BJ);
             }
             for (int32_t c : list) pos[c] = -1;
         }
@@ -522,6 +522,15 @@ HostBsr spgemm(const HostBsr& X, const HostBsr& Y) {
     return Z;
 }
 
+HostBsr spgemm(const HostBsr& X, const HostBsr& Y) {
+    if (X.br == 3 && X.bc == 3 && Y.bc == kModes) return spgemm_t<3, 3, kModes>(X, Y);
+    if (X.br == kModes && X.bc == 3 && Y.bc == kModes) return spgemm_t<kModes, 3, kModes>(X, Y);
+    return spgemm_t<kModes, kModes, kModes>(X, Y);  // the only other shape the setup forms
+}
+
+// R = P^T.  Rows are cut into one chunk per thread; each thread counts its chunk's columns,
+// the (column, chunk) prefix sums give every entry its place, and the threads scatter their
+// chunks, so each column of P lists its rows in ascending order whatever the thread count.
 HostBsr transpose(const HostBsr& P) {
     HostBsr R;
     R.n = P.m;
@@ -529,21 +538,41 @@ HostBsr transpose(const HostBsr& P) {
     R.br = P.bc;
     R.bc = P.br;
     const int br = P.br, bc = P.bc;
+    const int nt = std::max(1, omp_get_max_threads());
+    std::vector<int64_t> cut(nt + 1, 0);
+    for (int t = 0; t <= nt; ++t) cut[t] = P.n * t / nt;
+    std::vector<int64_t> cnt(size_t(nt) * (R.n + 1), 0);  // [chunk][column]
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        int64_t* c = cnt.data() + size_t(t) * (R.n + 1);
+        for (int64_t l = P.ptr[cut[t]]; l < P.ptr[cut[t + 1]]; ++l) ++c[P.col[l]];
+    }
     R.ptr.assign(R.n + 1, 0);
-    for (int64_t l = 0; l < P.nnzb(); ++l) ++R.ptr[P.col[l] + 1];
-    for (int64_t j = 0; j < R.n; ++j) R.ptr[j + 1] += R.ptr[j];
-    std::vector<int64_t> cur(R.ptr.begin(), R.ptr.end() - 1);
+    std::vector<int64_t> start(size_t(nt) * (R.n + 1), 0);
+    int64_t acc = 0;
+    for (int64_t j = 0; j < R.n; ++j) {
+        R.ptr[j] = acc;
+        for (int t = 0; t < nt; ++t) {
+            start[size_t(t) * (R.n + 1) + j] = acc;
+            acc += cnt[size_t(t) * (R.n + 1) + j];
+        }
+    }
+    R.ptr[R.n] = acc;
     R.col.assign(P.nnzb(), 0);
     R.val.assign(P.val.size(), 0.0);
-    for (int64_t i = 0; i < P.n; ++i)
-        for (int64_t l = P.ptr[i]; l < P.ptr[i + 1]; ++l) {
-            const int64_t q = cur[P.col[l]]++;
-            R.col[q] = int32_t(i);
-            const double* s = P.val.data() + l * br * bc;
-            double* d = R.val.data() + q * br * bc;
-            for (int r = 0; r < br; ++r)
-                for (int c = 0; c < bc; ++c) d[c * br + r] = s[r * bc + c];
-        }
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        int64_t* cur = start.data() + size_t(t) * (R.n + 1);
+        for (int64_t i = cut[t]; i < cut[t + 1]; ++i)
+            for (int64_t l = P.ptr[i]; l < P.ptr[i + 1]; ++l) {
+                const int64_t q = cur[P.col[l]]++;
+                R.col[q] = int32_t(i);
+                const double* s = P.val.data() + l * br * bc;
+                double* d = R.val.data() + q * br * bc;
+                for (int r = 0; r < br; ++r)
+                    for (int c = 0; c < bc; ++c) d[c * br + r] = s[r * bc + c];
+            }
+    }
     return R;
 }
 
@@ -831,6 +860,12 @@ extern "C" int fem_amg_setup(int64_t n_brow, const int32_t* indptr, const int32_
 }
 
 extern "C" int fem_amg_num_levels(const fem_amg* h) { return h ? int(h->lv.size()) : 0; }
+
+extern "C" int fem_amg_setup_phases(const fem_amg* h, double* seconds6) {
+    FEM_REQUIRE(h && seconds6, "NULL argument");
+    for (int i = 0; i < 6; ++i) seconds6[i] = h->setup_s[i];
+    return FEM_OK;
+}
 
 extern "C" int fem_amg_get_level(const fem_amg* h, int level, fem_amg_level_info* info) {
     FEM_REQUIRE(h && info, "NULL argument");

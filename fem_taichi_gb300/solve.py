@@ -86,6 +86,13 @@ class AmgHierarchy:
                         "lmax": info.lmax, "omega": info.omega, "setup_s": info.setup_s})
         return out
 
+    def setup_phases(self):
+        """Host seconds per setup phase (summed over levels)."""
+        t = (ctypes.c_double * 6)()
+        _lib.check(self.lib.fem_amg_setup_phases(self.h, t), "fem_amg_setup_phases")
+        return dict(zip(("strength_aggregation", "tentative", "lanczos", "smoothing", "galerkin", "coarse_inverse"),
+                        (round(v, 3) for v in t)))
+
     def export(self, level, what):
         """Host copy of one level's array (see fem_amg_export): a scipy BSR-like triple
         (indptr, indices, blocks) for what in 0..2, else the value / index array."""

@@ -99,7 +99,7 @@ def amg_setup(S: DeviceSystem, **opts):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t
     lv = H.levels()
-    return {"setup_s": H.setup_s, "upload_s": H.upload_s, "wall_s": wall,
+    return {"setup_s": H.setup_s, "upload_s": H.upload_s, "wall_s": wall, "phases_s": H.setup_phases(),
             "levels": [(l["n"], l["b"], l["nnzb_A"] or None) for l in lv],
             "operator_complexity": (S.nnzb * 9 + sum(l["nnzb_A"] * 36 for l in lv[1:])) / (S.nnzb * 9)}
 

@@ -320,6 +320,10 @@ typedef struct fem_amg_level_info {
     double setup_s;   /* host seconds spent building this level's transfer and coarse operator */
 } fem_amg_level_info;
 int fem_amg_num_levels(const fem_amg* amg);
+/* Host seconds of the setup phases summed over the levels: [0] strength + aggregation,
+ * [1] tentative prolongator, [2] Lanczos, [3] prolongator smoothing, [4] Galerkin products,
+ * [5] dense coarsest inverse. */
+int fem_amg_setup_phases(const fem_amg* amg, double* seconds6);
 int fem_amg_get_level(const fem_amg* amg, int level, fem_amg_level_info* info);
 /* Host copies of one level's arrays.  what: 0 A (levels >= 1), 1 P, 2 R = P^T, 3 the inverse
  * diagonal blocks (vals [n][b][b]), 4 the aggregate of each node (indices [n], -1 = none),
