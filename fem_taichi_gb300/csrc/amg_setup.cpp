@@ -120,34 +120,44 @@ int64_t diag_inverse(const HostBsr& A, const std::vector<int64_t>& dpos, std::ve
     return bad;
 }
 
-// y = A x (square, b x b blocks)
-void spmv(const HostBsr& A, const double* x, double* y) {
-    const int b = A.br, bb = b * b;
+// y = A x (square, B x B blocks)
+template <int B>
+void spmv_t(const HostBsr& A, const double* __restrict__ x, double* __restrict__ y) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < A.n; ++i) {
-        double acc[kModes] = {0, 0, 0, 0, 0, 0};
+        double acc[B] = {};
         for (int64_t l = A.ptr[i]; l < A.ptr[i + 1]; ++l) {
-            const double* a = A.val.data() + l * bb;
-            const double* xc = x + int64_t(A.col[l]) * b;
-            for (int r = 0; r < b; ++r)
-                for (int c = 0; c < b; ++c) acc[r] += a[r * b + c] * xc[c];
+            const double* a = A.val.data() + l * B * B;
+            const double* xc = x + int64_t(A.col[l]) * B;
+            for (int r = 0; r < B; ++r)
+                for (int c = 0; c < B; ++c) acc[r] += a[r * B + c] * xc[c];
         }
-        for (int r = 0; r < b; ++r) y[i * b + r] = acc[r];
+        for (int r = 0; r < B; ++r) y[i * B + r] = acc[r];
     }
 }
 
-// y = blockdiag(M) x, M [n][b][b]
-void block_apply(int64_t n, int b, const double* M, const double* x, double* y) {
-    const int bb = b * b;
+void spmv(const HostBsr& A, const double* x, double* y) {
+    if (A.br == 3) spmv_t<3>(A, x, y);
+    else spmv_t<kModes>(A, x, y);
+}
+
+// y = blockdiag(M) x, M [n][B][B]
+template <int B>
+void block_apply_t(int64_t n, const double* __restrict__ M, const double* __restrict__ x, double* __restrict__ y) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-        const double* m = M + i * bb;
-        for (int r = 0; r < b; ++r) {
+        const double* m = M + i * B * B;
+        for (int r = 0; r < B; ++r) {
             double s = 0.0;
-            for (int c = 0; c < b; ++c) s += m[r * b + c] * x[i * b + c];
-            y[i * b + r] = s;
+            for (int c = 0; c < B; ++c) s += m[r * B + c] * x[i * B + c];
+            y[i * B + r] = s;
         }
     }
+}
+
+void block_apply(int64_t n, int b, const double* M, const double* x, double* y) {
+    if (b == 3) block_apply_t<3>(n, M, x, y);
+    else block_apply_t<kModes>(n, M, x, y);
 }
 
 double dot(const std::vector<double>& a, const std::vector<double>& b) {
