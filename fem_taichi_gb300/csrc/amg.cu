@@ -586,7 +586,9 @@ int upload_bsr(const HostBsr& H, DevBsr& D) {
     if ((rc = upload_array(p, &D.ptr))) return rc;
     if ((rc = upload_array(H.col, &D.col))) return rc;
     if ((rc = upload_array(v, &D.val))) return rc;
-    std::vector<float> vb(H.val.begin(), H.val.end());
+    std::vector<float> vb(H.val.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < int64_t(vb.size()); ++e) vb[e] = float(H.val[e]);
     return upload_array(vb, &D.valb);
 }
 
