@@ -65,11 +65,15 @@ def write_tecplot_ascii(output_file, title, Physics, Fields, Field_names):
             head.append(',"' + " " + str(name) + str(step + 1) + '"')  # ("%s " % ',"') + name + step + '"'
     head.append("\n")
     head.append("ZONE  I=" + str(N) + ", J=" + str(conn.shape[0]) + ", F=FEPOINT, ET=BRICK\n")
-    txt = np.char.mod("%10.5e", data)
-    txt[np.isnan(data)] = ""
+    # one format string per row; rows holding NaN (written as empty fields) go value by value
+    fmt = " ".join(["%10.5e"] * data.shape[1])
+    nan_rows = np.isnan(data).any(axis=1)
+    rows = data.tolist()
+    lines = [(" ".join("" if v != v else "%10.5e" % v for v in r) if bad else fmt % tuple(r))
+             for r, bad in zip(rows, nan_rows.tolist())]
     with open(output_file, "w") as f:
         f.write("".join(head))
-        f.write("\n".join(" ".join(r) for r in txt))
+        f.write("\n".join(lines))
         f.write("\n")
         f.write("\n".join(" ".join(map(str, r)) for r in conn.tolist()))
         f.write("\n")

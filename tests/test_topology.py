@@ -164,3 +164,23 @@ def test_tecplot_ascii_output(tmp_path):
     assert np.allclose(vals, ref, rtol=1e-5)
     conn = np.array([[int(x) for x in r.split(" ")] for r in lines[3 + P.Num_Node:]])
     assert np.array_equal(conn, P.conn + 1)
+
+
+def test_tecplot_ascii_rows_and_nan_fields(tmp_path):
+    """Node rows: x y z then every field of every step, '%10.5e' each, space separated, NaN
+    as an empty field (POST_process.py:101-135)."""
+    from fem_taichi_gb300.post import write_tecplot_ascii
+    P = F.hex_block(3, 2, 2, jitter=0.1, seed=1, fix="zmin")
+    N = P.Num_Node
+    Fld = np.random.default_rng(0).standard_normal((N, 2, 2))
+    Fld[1, 0, 1] = np.nan
+    Fld[4, :, :] = np.nan
+    out = tmp_path / "t.dat"
+    write_tecplot_ascii(str(out), "t", P, Fld, ["a", "b"])
+    lines = out.read_text().splitlines()
+    body = lines[3:3 + N]
+    data = np.concatenate((P.Node[-3:].T, Fld.transpose(0, 2, 1).reshape(N, -1)), axis=-1)
+    for i in (0, 1, 4, N - 1):
+        want = " ".join("" if np.isnan(v) else "%10.5e" % v for v in data[i])
+        assert body[i] == want
+    assert len(lines) == 3 + N + P.Num_Elem
