@@ -6,20 +6,23 @@ Workload (default): the 200x200x24-element seeded jittered steel block (1,010,02
 centrifugal term for Omegas=(0,0,100), bottom face penalised.  A step is one pass of the
 path over that mesh: the element-integral kernel and the deterministic gather kernel.
 
-  value  : device-resident throughput (inputs already in HBM), CUDA events on the launch
-           stream, W warm-up steps then K timed steps, max over ranks.
+  value  : device-resident throughput of the FP64 kernels (the reference computes in f64
+           throughout; FEM_model_csr.py:33), inputs already in HBM, CUDA events on the
+           launch stream, W warm-up steps then K timed steps, max over ranks.
   e2e    : the same metric through the public Python API with host buffers: per step the
            node coordinates are copied host->device from pinned memory, then
            Model.Get_MatrixKL(), Get_MatrixM() and Get_VectorF() return scipy/numpy objects
-           (device->host copies included).
+           (device->host copies included), FP64 kernels.
   roofline: algorithmic bytes of one assembly (24N + 32E + 80 nnzb + 24N + 4 nnzb + 4(N+1))
-           / measured time, against the measured HBM copy bandwidth.  Beside it, the element
-           kernel's arithmetic rate in FP64-equivalent operations and its ratio to the
-           measured FP64 pipe rate (the double-float kernel exceeds the FP64 pipe; it is
-           bound by FP32 instruction issue).
+           / measured time, against the measured HBM copy bandwidth; and, because the FP64
+           element kernel is bound by the FP64 pipe, its FP64 operation rate against the
+           FP64 FMA rate measured on the same device ("binding": "fp64").
+  double_float: the same assembly with the double-float kernels (pairs of FP32 on the FP32
+           pipes, about 48-bit significands) -- faster, reported separately, not FP64.
   cpu_baseline / --impl reference: the C restatement of the reference algorithm (element
            loop, per-element scratch, linear-search slot lookup, atomic scatter, penalty)
-           on all host cores.
+           on all host cores, on the same 200x200x24 mesh, its pattern built by the oracle's
+           restatement of Read.pre_process (scipy); the product library is not loaded.
 
 Multi-GPU (torchrun): every rank assembles its own replica of the workload (weak scaling,
 no data-path collective); value = all ranks' elements / the slowest rank's time.
@@ -43,12 +46,15 @@ sys.path.insert(0, ROOT)
 METRIC = "K+M assembly Melem/s"
 UNIT = "Melem/s"
 
-# Arithmetic of one element's integrals in FP64 operations, counted from the FP64 kernel
-# k_hex8_element (the double-float kernel evaluates the same operations in FP32 pairs):
+# FP64 operations of one element's integrals (FMA = 2), counted from k_hex8_element:
 # phase A per Gauss point: J 72 FMA, adjugate 18, det 3, reciprocal ~10, R 72 (24x3),
 # R/det 24, load density ~40; phase B: 28 off-diagonal pairs x (72 + 4 + 21 + 1) +
-# 8 diagonal pairs x (48 + 8 + 14) + F 192.  Flops count an FMA as 2.
+# 8 diagonal pairs x (48 + 8 + 14) + F 192.
 ELEM_FP64_FLOPS = 2 * 8 * (72 + 72 + 24) + 8 * (18 + 3 + 10 + 40) + 28 * (2 * 76 + 21 + 1) + 8 * (2 * 56 + 14) + 2 * 192
+# FP64 operations of one element of the stress element kernel (k_stress_element): per Gauss
+# point J and the displacement gradient 144 FMA, adjugate 27, det 5, reciprocal ~10, H 63,
+# stresses 18; extrapolation to the 8 corners 8 x 6 x 8 FMA.
+STRESS_ELEM_FP64_FLOPS = 8 * (2 * 144 + 27 + 5 + 10 + 63 + 18) + 2 * 8 * 6 * 8
 
 
 def parse():
@@ -58,12 +64,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--algo", choices=["dd", "fp64"], default="dd", help="assembly arithmetic")
+    ap.add_argument("--no-dd", action="store_true", help="skip the double-float assembly line")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--no-solve", action="store_true", help="skip the c3/c4 static-solve studies")
+    ap.add_argument("--no-solve", action="store_true", help="skip the static-solve studies")
     ap.add_argument("--no-c5", action="store_true", help="skip the 32-RHS twisted-slab (c5) solve study")
     return ap.parse_args()
 
@@ -80,6 +86,33 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def fma_rate_tflops(fp64: bool, stream_handle) -> float:
+    """FMA throughput of this device (TFLOP/s) from the benchmark's probe library."""
+    from fem_taichi_gb300 import build as B
+    L = ctypes.CDLL(B.build_probe())
+    L.fem_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+    L.fem_probe_fma_tflops.restype = ctypes.c_int
+    r = ctypes.c_double(0)
+    rc = L.fem_probe_fma_tflops(1 if fp64 else 0, ctypes.byref(r), stream_handle)
+    if rc != 0:
+        raise RuntimeError(f"FMA rate probe failed (CUDA error {rc})")
+    return r.value
+
+
+def native_libraries():
+    """Shared libraries of this repository mapped into the process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for ln in f:
+                p = ln.split()[-1] if ln.strip() else ""
+                if p.startswith(ROOT) and ".so" in p:
+                    out.add(os.path.relpath(p, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
 
 
 class ClockSampler:
@@ -172,32 +205,40 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def mesh_bc_arrays(P):
-    bn = np.concatenate([P.Nind[np.asarray(b[0])] for b in P.Bounds]) if P.Bounds else np.zeros(0, np.int64)
-    bc = np.zeros((bn.size, 3))
-    return bn, bc
+def workload_name(cfg, grid, N, E, nnzb):
+    return (f"{cfg}: hex8 K+M+F assembly, {grid[0]}x{grid[1]}x{grid[2]} elements ({N:,} nodes, "
+            f"{E:,} elements, nnzb {nnzb:,}), FP64, BSR")
 
 
-def cpu_sample_mesh(cfg):
-    """Bounded CPU sample of a workload: the same block family (element shape, jitter,
-    density, material, loads) with the x/y element counts halved until it has at most
-    240,000 elements."""
-    import fem_taichi_gb300 as F
-    kw = dict(F.CONFIGS[cfg])
-    while kw["nx"] * kw["ny"] * kw["nz"] > 240_000:
-        kw["nx"] //= 2
-        kw["ny"] //= 2
-        kw["size"] = (kw["size"][0] / 2, kw["size"][1] / 2, kw["size"][2])
-    return F.hex_block(name=cfg + "-sample", **kw)
+# ---------------------------------------------------------------------------------------------
+# CPU side: the reference algorithm's C restatement on the same mesh
+# ---------------------------------------------------------------------------------------------
+def reference_mesh(cfg):
+    """The workload's mesh with its pattern built by the oracle's restatement of
+    Read.pre_process (READ_physics.py:42-61, scipy): no product library is loaded."""
+    from fem_taichi_gb300.mesh import CONFIGS, block_arrays
+    from oracle import fem_oracle as O
+    kw = CONFIGS[cfg]
+    b = block_arrays(**kw)
+    N = b["ids"].size
+    Node = np.zeros((6, N))
+    Node[0] = b["ids"]
+    Node[3:] = b["xyz"].T
+    topo = O.pre_process(Node, b["elem"])
+    nind = topo["Nind"]
+    conn = np.ascontiguousarray(nind[b["elem"]].T, dtype=np.int32)
+    bn = np.concatenate([nind[np.asarray(g[0])] for g in b["bounds"]]) if b["bounds"] else np.zeros(0, np.int64)
+    return {"xyz": np.ascontiguousarray(b["xyz"]), "conn": conn, "SmNode": topo["SmNode"].astype(np.int32),
+            "ReNode": topo["ReNode"].astype(np.int32), "CoElem": topo["CoElem"].astype(np.int32), "N": N,
+            "E": conn.shape[0], "nnzb": int(topo["SmNode"][-1]), "bn": bn, "bc": np.zeros((bn.size, 3)),
+            "grid": (kw["nx"], kw["ny"], kw["nz"])}
 
 
-def run_cpu_port(P, mat, om, steps, warmup, threads):
+def time_cpu_port(R, mat, om, steps, warmup, threads):
     """Times the C restatement of the reference algorithm (all threads); returns s/step."""
     from oracle import c_oracle as C
-    bn, bc = mesh_bc_arrays(P)
-    nnzb = int(P.SmNode[-1])
-    out = (np.zeros((nnzb, 3, 3)), np.zeros(nnzb), np.zeros((P.Num_Node, 3)))
-    args = (P.xyz, P.conn, P.SmNode, P.ReNode, mat, om, bn, bc)
+    out = (np.zeros((R["nnzb"], 3, 3)), np.zeros(R["nnzb"]), np.zeros((R["N"], 3)))
+    args = (R["xyz"], R["conn"], R["SmNode"], R["ReNode"], mat, om, R["bn"], R["bc"])
     for _ in range(warmup):
         C.assemble(*args, nthreads=threads, out=out)
     t0 = time.perf_counter()
@@ -210,28 +251,110 @@ def reference_arm(a):
     ws, rank, _ = dist_setup("gloo")
     if rank != 0:
         return
-    import fem_taichi_gb300 as F
-    P = F.config_mesh(a.config)
-    S = cpu_sample_mesh(a.config)
+    from fem_taichi_gb300.mesh import STEEL
+    R = reference_mesh(a.config)
     thr = cpu_threads()
-    t = run_cpu_port(S, F.STEEL, (0, 0, 100), a.steps, a.warmup, thr)
-    v = S.Num_Elem / t / 1e6
+    t = time_cpu_port(R, STEEL, (0, 0, 100), a.steps, a.warmup, thr)
+    v = R["E"] / t / 1e6
+    name = workload_name(a.config, R["grid"], R["N"], R["E"], R["nnzb"])
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(a.config, P), "threads": thr},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered hex block, steel, Omegas=(0,0,100))",
+            "config": {"workload": name, "threads": thr, "same_config": True},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
-                             "sample": f"{S.grid[0]}x{S.grid[1]}x{S.grid[2]} block of the {a.config} family "
-                                       f"({S.Num_Elem:,} elements, K+M+F) per step, {a.steps} steps"},
+                             "sample": f"the full {a.config} mesh ({R['E']:,} elements, K+M+F) per step, "
+                                       f"{a.steps} steps after {a.warmup} warm-up"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": ("reference (Python/Taichi 0.6.28 + MKL Pardiso) cannot run on this image; timed: C restatement "
-                     "of its algorithm (oracle/fem_oracle.c) with OpenMP atomics on all host cores")}
+            "native_so_loaded": native_libraries(),
+            "note": ("reference (Python/Taichi 0.6.28 + MKL Pardiso) cannot run at this size here: taichi is not "
+                     "installed; timed: C restatement of its algorithm (oracle/fem_oracle.c, OpenMP atomics, all "
+                     "host cores), whose numpy twin is pinned to the reference's own outputs")}
     print(json.dumps(line), flush=True)
 
 
-def workload_name(cfg, P):
-    return (f"{cfg}: hex8 K+M+F assembly, {P.grid[0]}x{P.grid[1]}x{P.grid[2]} elements ({P.Num_Node:,} nodes, "
-            f"{P.Num_Elem:,} elements, nnzb {int(P.SmNode[-1]):,}), FP64, BSR")
+# ---------------------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------------------
+def time_assembly(L, _lib, model, algo, steps, warmup, dev, clocks=None, ws=1):
+    """Times `steps` device-resident assemblies (element + gather kernels) with CUDA events
+    on the launch stream; returns (total_ms over ranks, mean element ms, mean gather ms, clocks)."""
+    import torch
+    from fem_taichi_gb300.model import _dptr, _stream
+    N, nnzb = model.Num_Node, model.mesh.nnzb
+    Kt = torch.empty((nnzb, 3, 3), dtype=torch.float64, device=dev)
+    Mt = torch.empty((nnzb,), dtype=torch.float64, device=dev)
+    Ft = torch.empty((N, 3), dtype=torch.float64, device=dev)
+    wsb = model.workspace()
+    code = _lib.ALGO_DD if algo == "dd" else _lib.ALGO_FP64
+    out = _lib.FemAssemblyOut(_lib.LAYOUT_BSR, _lib.LAYOUT_BSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
+                              model.fixed.data_ptr(), model.loads.data_ptr(), code)
+    st = _stream(dev)
+    stream = torch.cuda.current_stream(dev)
+    mesh_c, mat_c = ctypes.byref(model.mesh.c), ctypes.byref(model.mat)
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(L.fem_assemble_elements(mesh_c, mat_c, code, _dptr(wsb), wsb.numel(), st), "elements")
+        if ev is not None:
+            ev[1].record(stream)
+        _lib.check(L.fem_assemble_gather(mesh_c, ctypes.byref(out), _dptr(wsb), wsb.numel(), st), "gather")
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    if clocks is not None:
+        clocks.start()
+        time.sleep(0.25)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(steps):
+        step(evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop() if clocks is not None else None
+    total_ms = max_over_ranks(t0.elapsed_time(t1), dev)
+    el_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    ga_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    del Kt, Mt, Ft
+    return total_ms, el_ms, ga_ms, clk
+
+
+def time_stress(post, N, dev, reps=5):
+    import torch
+    Sout = torch.empty((N, 10), dtype=torch.float64, device=dev)
+    for _ in range(2):
+        post.stress_device(Sout)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(reps):
+        post.stress_device(Sout)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    return s0.elapsed_time(s1) / reps
+
+
+def traffic_record(kind):
+    """DRAM bytes per assembly of the given kernels from the committed ncu summary."""
+    tf = os.path.join(ROOT, "profiles", "assembly_c2_traffic.json")
+    if not os.path.exists(tf):
+        return None
+    with open(tf) as f:
+        d = json.load(f)
+    r = d.get(kind)
+    return r.get("dram_bytes_per_assembly") if isinstance(r, dict) else None
 
 
 def main():
@@ -244,98 +367,66 @@ def main():
     dev = torch.device("cuda", local)
     import fem_taichi_gb300 as F
     from fem_taichi_gb300 import _lib
-    from fem_taichi_gb300.model import _dptr, _stream
+    from fem_taichi_gb300.model import _stream
     L = _lib.load()
     mat, om = F.STEEL, (0, 0, 100)
     t_mesh = time.perf_counter()
     P = F.config_mesh(a.config)
     t_mesh = time.perf_counter() - t_mesh
     N, E, nnzb = P.Num_Node, P.Num_Elem, int(P.SmNode[-1])
-    model = F.Model(a.config, P, mat, Omegas=om, device=dev)
-    Kt = torch.empty((nnzb, 3, 3), dtype=torch.float64, device=dev)
-    Mt = torch.empty((nnzb,), dtype=torch.float64, device=dev)
-    Ft = torch.empty((N, 3), dtype=torch.float64, device=dev)
-    wsb = model.workspace()
-    algo = _lib.ALGO_DD if a.algo == "dd" else _lib.ALGO_FP64
-    out = _lib.FemAssemblyOut(_lib.LAYOUT_BSR, _lib.LAYOUT_BSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
-                              model.fixed.data_ptr(), model.loads.data_ptr(), algo)
+    model = F.Model(a.config, P, mat, Omegas=om, device=dev, algo="fp64")
     st = _stream(dev)
-    stream = torch.cuda.current_stream(dev)
-    mesh_c, mat_c = ctypes.byref(model.mesh.c), ctypes.byref(model.mat)
+    smi = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+    clocks = ClockSampler(int(smi) if smi.isdigit() else local)
 
-    def step(ev=None):
-        if ev is not None:
-            ev[0].record(stream)
-        _lib.check(L.fem_assemble_elements(mesh_c, mat_c, algo, _dptr(wsb), wsb.numel(), st), "elements")
-        if ev is not None:
-            ev[1].record(stream)
-        _lib.check(L.fem_assemble_gather(mesh_c, ctypes.byref(out), _dptr(wsb), wsb.numel(), st), "gather")
-        if ev is not None:
-            ev[2].record(stream)
-
-    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
-                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
-    for _ in range(a.warmup):
-        step()
-    torch.cuda.synchronize()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(a.steps)]
-    clocks.start()
-    time.sleep(0.25)
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for k in range(a.steps):
-        step(evs[k])
-    t1.record(stream)
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    clk = clocks.stop()
-    total_ms = t0.elapsed_time(t1)
-    el_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
-    ga_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
-    total_ms = max_over_ranks(total_ms, dev)
+    # -- headline: FP64 kernels -----------------------------------------------------------------
+    total_ms, el_ms, ga_ms, clk = time_assembly(L, _lib, model, "fp64", a.steps, a.warmup, dev, clocks, ws)
     ms_step = total_ms / a.steps
     value = whole_job_rate(ws, E * a.steps, total_ms * 1e-3)
 
-    # -- roofline ---------------------------------------------------------------------------
+    # -- roofline -----------------------------------------------------------------------------
     peak, peak_kind = measured_peaks()
     ab = algorithmic_bytes(N, E, nnzb)
     achieved = ab / (ms_step * 1e-3) / 1e9
-    fp64_peak = ctypes.c_double(0)
-    _lib.check(L.fem_diag_fp64_tflops(ctypes.byref(fp64_peak), st), "fp64 probe")
+    fp64_peak = fma_rate_tflops(True, st)
+    fp32_peak = fma_rate_tflops(False, st)
     fp64_ach = E * ELEM_FP64_FLOPS / (el_ms * 1e-3) / 1e12
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "assembly_c2_traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get("dram_bytes_per_assembly")
-
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded jittered hex block, steel, Omegas=(0,0,100))",
-            "config": {"workload": workload_name(a.config, P), "n_node": N, "n_elem": E, "nnzb": nnzb,
+            "config": {"workload": workload_name(a.config, P.grid, N, E, nnzb), "n_node": N, "n_elem": E,
+                       "nnzb": nnzb, "arith": "FP64 (FP64 pipe)",
                        "layout": "BSR K [nnzb][3][3], M [nnzb], F [N][3]",
-                       "l2": "inputs+outputs+workspace ~5.4 GB per step >> 129 MB L2 (no flush needed)",
+                       "l2": "inputs+outputs+workspace ~5 GB per step >> 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "fem_assemble = k_hex8_element + k_gather (one assembly)",
+                         "frac": achieved / peak, "traffic": traffic_record("fp64"), "peak_kind": peak_kind,
+                         "kernel": "fem_assemble = k_hex8_element + k_gather (one assembly, FP64)",
                          "algorithmic_bytes": ab,
-                         "element_arith": {
-                             "kernel": "k_hex8_element_dd" if a.algo == "dd" else "k_hex8_element",
-                             "arith": "double-float pairs on the FP32 pipes" if a.algo == "dd" else "FP64 pipe",
-                             "fp64_equivalent_tflops": fp64_ach, "fp64_ops_per_elem": ELEM_FP64_FLOPS,
-                             "fp64_pipe_peak_tflops_measured": fp64_peak.value,
-                             "x_fp64_pipe_peak": fp64_ach / fp64_peak.value}},
+                         "binding": "fp64",
+                         "fp64": {"kernel": "k_hex8_element", "flops_per_elem": ELEM_FP64_FLOPS,
+                                  "achieved_tflops": fp64_ach, "peak_tflops": fp64_peak,
+                                  "peak_kind": "measured FP64 FMA rate of this device (fem_probe_fma_tflops)",
+                                  "frac_fp64": fp64_ach / fp64_peak,
+                                  "element_share": el_ms / (el_ms + ga_ms)}},
             "kernels": {"k_hex8_element_ms": el_ms, "k_gather_ms": ga_ms,
                         "share_element": el_ms / (el_ms + ga_ms), "share_gather": ga_ms / (el_ms + ga_ms)},
             "gpu_launches": 2 * a.steps, "clocks": clk}
 
-    # -- e2e through the public API -------------------------------------------------------------
+    # -- the double-float kernels, separately ------------------------------------------------
+    if not a.no_dd:
+        t_dd, el_dd, ga_dd, _ = time_assembly(L, _lib, model, "dd", a.steps, a.warmup, dev, None, ws)
+        ms_dd = t_dd / a.steps
+        line["double_float"] = {
+            "arith": "double-float (48-bit): FP32 pairs on the FP32 pipes", "value": whole_job_rate(ws, E * a.steps,
+                                                                                                    t_dd * 1e-3),
+            "unit": UNIT, "ms_per_step": ms_dd, "k_hex8_element_dd_ms": el_dd, "k_gather_dd_ms": ga_dd,
+            "hbm_frac": algorithmic_bytes(N, E, nnzb) / (ms_dd * 1e-3) / 1e9 / peak,
+            "traffic": traffic_record("dd"),
+            "fp64_equivalent_tflops": E * ELEM_FP64_FLOPS / (el_dd * 1e-3) / 1e12,
+            "fp32_fma_peak_tflops": fp32_peak, "gpu_launches": 2 * a.steps}
+
+    # -- e2e through the public API (FP64 kernels) ----------------------------------------------
     if not a.no_e2e:
         ne = a.e2e_steps or max(3, min(a.steps, 10))
         xyz_h = torch.from_numpy(P.xyz.copy()).pin_memory()
@@ -358,35 +449,32 @@ def main():
             r = e2e_step()
             del r
         torch.cuda.synchronize()
-        w1 = time.perf_counter() - w0
-        w1 = max_over_ranks(w1, dev)
+        w1 = max_over_ranks(time.perf_counter() - w0, dev)
         line["e2e"] = {"value": whole_job_rate(ws, E * ne, w1), "unit": UNIT, "h2d_bytes_per_step": 24 * N,
                        "d2h_bytes_per_step": 72 * nnzb + 24 * nnzb + 24 * N, "steps": ne,
-                       "ms_per_step": w1 / ne * 1e3,
-                       "path": "Model.set_coordinates(pinned) + Get_MatrixKL + Get_MatrixM + Get_VectorF"}
-        line["e2e"]["gpu_launches"] = 2 * ne
+                       "ms_per_step": w1 / ne * 1e3, "arith": "FP64",
+                       "path": "Model.set_coordinates(pinned) + Get_MatrixKL + Get_MatrixM + Get_VectorF",
+                       "gpu_launches": 2 * ne * model.pipeline_parts}
 
     # -- extras: stress recovery on the same mesh -------------------------------------------------
     if not a.no_extras:
         u = np.random.default_rng(2).uniform(-1e-3, 1e-3, size=(N, 3))
-        post = F.Post(a.config, P, mat, u, mesh=model.mesh)
-        Sout = torch.empty((N, 10), dtype=torch.float64, device=dev)
-        for _ in range(2):
-            post.stress_device(Sout)
-        torch.cuda.synchronize()
-        s0 = torch.cuda.Event(enable_timing=True)
-        s1 = torch.cuda.Event(enable_timing=True)
-        ns = 5
-        s0.record(stream)
-        for _ in range(ns):
-            post.stress_device(Sout)
-        s1.record(stream)
-        torch.cuda.synchronize()
-        sms = s0.elapsed_time(s1) / ns
         sbytes = 24 * N + 24 * N + 32 * E + 80 * N + 4 * (N + 1) + 32 * E + 4 * N
-        line["stress"] = {"ms": sms, "algorithmic_bytes": sbytes, "gbs": sbytes / (sms * 1e-3) / 1e9,
-                          "frac_hbm": sbytes / (sms * 1e-3) / 1e9 / peak, "Mnodes_per_s": N / sms / 1e3}
-        line["stress"]["gpu_launches"] = 2 * ns
+        post = F.Post(a.config, P, mat, u, mesh=model.mesh, algo="fp64")
+        sms = time_stress(post, N, dev)
+        st_ach = E * STRESS_ELEM_FP64_FLOPS / (sms * 1e-3) / 1e12
+        line["stress"] = {"ms": sms, "arith": "FP64", "algorithmic_bytes": sbytes,
+                          "gbs": sbytes / (sms * 1e-3) / 1e9, "frac_hbm": sbytes / (sms * 1e-3) / 1e9 / peak,
+                          "Mnodes_per_s": N / sms / 1e3, "binding": "fp64",
+                          "fp64": {"flops_per_elem": STRESS_ELEM_FP64_FLOPS, "achieved_tflops": st_ach,
+                                   "frac_fp64": st_ach / fp64_peak,
+                                   "note": "element-kernel operations over the time of both stress kernels"},
+                          "gpu_launches": 2 * 5}
+        post_dd = F.Post(a.config, P, mat, u, mesh=model.mesh, algo="dd")
+        sdd = time_stress(post_dd, N, dev)
+        line["stress"]["double_float"] = {"ms": sdd, "gbs": sbytes / (sdd * 1e-3) / 1e9,
+                                          "Mnodes_per_s": N / sdd / 1e3}
+        del post, post_dd
         line["host_setup_s"] = {"mesh_and_pattern": t_mesh}
         # topology (incidence + block pattern + gather map): host C++ build vs device build
         from fem_taichi_gb300 import mesh as M_
@@ -408,11 +496,11 @@ def main():
 
     # -- static solve studies (seconds to 1e-8 relative error vs an FP64 reference) ---------------
     if not a.no_solve and rank == 0:
-        from fem_taichi_gb300 import study
+        import bench_solve as study
 
         def brief(r):
-            keep = ("label", "wall_s", "iterations", "outer", "relres", "relerr", "meets_1e-8", "status_text",
-                    "ms_per_iteration", "nrhs")
+            keep = ("label", "wall_s", "iterations", "outer", "relres", "floor", "relerr", "meets_1e-8", "status_text",
+                    "ms_per_iteration", "nrhs", "setup_s")
             out = {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
             if "amg" in r:
                 out["amg_setup"] = r["amg"]
@@ -423,8 +511,9 @@ def main():
         sol["c3"]["spmv"] = r3["spmv"]
         r4, net = study.c4_study(device=dev)
         sol["c4"] = brief(r4)
-        sol["c4"]["training"] = r4["training"]
-        sol["c4"]["inference_s"] = r4["inference_s"]
+        for k in ("training", "inference_s", "gain"):
+            if k in r4:
+                sol["c4"][k] = r4[k]
         if not a.no_c5:
             r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=1000)
             sol["c5"] = brief(r5)
@@ -432,28 +521,26 @@ def main():
         sol["modal_c1"] = study.modal_study("c1", num_eigen=100, num_block=10, device=dev)
         line["solve"] = sol
 
-    # -- CPU baseline (rank 0, N = 1) -----------------------------------------------------------
+    # -- CPU baseline (rank 0, N = 1): the reference algorithm's C port on the same mesh ---------
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         thr = cpu_threads()
-        S = cpu_sample_mesh(a.config)
+        R = reference_mesh(a.config)
         ns = 8
-        t = run_cpu_port(S, mat, om, ns, 1, thr)
-        line["cpu_baseline"] = {"value": S.Num_Elem / t / 1e6, "unit": UNIT, "cores": thr, "kind": "port",
-                                "sample": f"{ns} assemblies (K+M+F) of the {S.grid[0]}x{S.grid[1]}x{S.grid[2]} "
-                                          f"block of the {a.config} family ({S.Num_Elem:,} elements) with "
-                                          f"oracle/fem_oracle.c on {thr} threads, {t:.2f} s each"}
+        t = time_cpu_port(R, mat, om, ns, 1, thr)
+        line["cpu_baseline"] = {"value": R["E"] / t / 1e6, "unit": UNIT, "cores": thr, "kind": "port",
+                                "sample": f"{ns} assemblies (K+M+F) of the full {a.config} mesh ({R['E']:,} "
+                                          f"elements) with oracle/fem_oracle.c on {thr} threads, {t:.2f} s each"}
         if not a.no_extras:
-            # stress recovery: the C restatement on the same sample mesh, all host threads
             from oracle import c_oracle as C
             from oracle import fem_oracle as O
-            us = np.random.default_rng(2).uniform(-1e-3, 1e-3, size=(S.Num_Node, 3))
-            W = O.extrapolation_table("written")
-            C.stress(S.xyz, S.conn, S.CoElem, mat, us, W, nthreads=thr)
+            us = np.random.default_rng(2).uniform(-1e-3, 1e-3, size=(R["N"], 3))
+            W = O.extrapolation_table("aliased")
+            C.stress(R["xyz"], R["conn"], R["CoElem"], mat, us, W, nthreads=thr)
             t0 = time.perf_counter()
-            C.stress(S.xyz, S.conn, S.CoElem, mat, us, W, nthreads=thr)
+            C.stress(R["xyz"], R["conn"], R["CoElem"], mat, us, W, nthreads=thr)
             ts = time.perf_counter() - t0
-            line["cpu_baseline"]["stress"] = {"Mnodes_per_s": S.Num_Node / ts / 1e6, "s": ts, "cores": thr,
-                                              "sample": f"{S.Num_Node:,} nodes of the same sample mesh"}
+            line["cpu_baseline"]["stress"] = {"Mnodes_per_s": R["N"] / ts / 1e6, "s": ts, "cores": thr,
+                                              "sample": f"all {R['N']:,} nodes of the same mesh"}
         if not a.no_solve:
             # static solve: FP64 block-Jacobi PCG with scipy products (1 thread) on the c3
             # system, a bounded sample of iterations scaled to the GPU FP64 solver's count
@@ -463,8 +550,8 @@ def main():
                          device=dev)
             K3, F3 = M3.Get_MatrixKL(), M3.Get_VectorF()
             _, it, tsol = SO.bj_pcg(K3, F3, rtol=1e-10, maxit=30)
-            gpu_it = next(r["iterations"] for r in line.get("solve", {}).get("c3", {}).get("solves", [])
-                          if r["label"] == "fp64_bj") if "solve" in line else None
+            gpu_it = next((r["iterations"] for r in line.get("solve", {}).get("c3", {}).get("solves", [])
+                           if r["label"] == "fp64_bj"), None)
             est = tsol / it * gpu_it if gpu_it else None
             line["cpu_baseline"]["solve"] = {
                 "kind": "port", "cores": 1, "s_per_iteration": tsol / it,
@@ -472,6 +559,7 @@ def main():
                 "sample": f"{it} FP64 block-Jacobi PCG iterations on c3 (214,221 nodes) with scipy products, "
                           f"scaled to the {gpu_it} iterations the same method takes to 1e-10; Pardiso "
                           "(the reference's solver) is not available"}
+    line["native_so_loaded"] = native_libraries()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

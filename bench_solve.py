@@ -23,10 +23,10 @@ import time
 import numpy as np
 import torch
 
-from . import mesh as _mesh
-from .learned import LearnedPreconditioner, NodeData
-from .model import Model
-from .solve import DeviceSystem
+from fem_taichi_gb300 import mesh as _mesh
+from fem_taichi_gb300.learned import LearnedPreconditioner, NodeData
+from fem_taichi_gb300.model import Model
+from fem_taichi_gb300.solve import DeviceSystem
 
 STEEL = _mesh.STEEL
 
@@ -276,34 +276,10 @@ def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, ma
             "amg": amg, "solves": rows}
 
 
-def solve_probe(cfg="c3", iterations=40, device="cuda", variant64=None, variant32=None):
-    """A short, eager (no CUDA graph) run of the solver kernels for launch-list profiling:
-    picks both SpMV launch variants (autotuned unless given: under a profiler the tuner's
-    timings are distorted), then runs `iterations` FP64 PCG iterations and `iterations` FP32
-    inner iterations in one refinement step."""
-    P = _mesh.config_mesh(cfg)
-    extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
-    S = DeviceSystem(Model(cfg, P, STEEL, device=device, extra_loads=extra))
-    if variant64 is not None:
-        S._variant[(False, 1)] = int(variant64)
-    if variant32 is not None:
-        S.K32()
-        S._variant[(True, 1)] = int(variant32)
-    S.variant(False, 1)
-    S.variant(True, 1)
-    out = []
-    for mixed in (False, True):
-        _, st = S.solve(rtol=1e-10, mixed=mixed, maxit=iterations, inner_maxit=iterations, max_outer=1,
-                        use_graph=False, unroll=8)
-        out.append(st)
-    torch.cuda.synchronize()
-    return out
-
-
 def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda", precond="amg"):
     """Block-Lanczos modal solve (SOLVE_eigen.py:45-89, the reference driver's num_eigen=100)
     on a config mesh: wall time of a warm solve and the lowest frequencies."""
-    from .eigen import Eigen_solver
+    from fem_taichi_gb300.eigen import Eigen_solver
     P = _mesh.config_mesh(cfg)
     M = Model(cfg, P, STEEL, device=device)
     solver = Eigen_solver(M)
@@ -320,3 +296,27 @@ def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda", precond="a
             "wall_s": wall,
             "steps": solver.last_stats["steps"], "solve_iterations": solver.last_stats["solve_iterations"],
             "lowest_freq_hz": [float(f) for f in freq[:5]], "M_orthonormality_err": orth}
+
+
+def profile_solve(cfg="c3", nrhs=1):
+    """One warm multigrid-preconditioned FP64 static solve bracketed by cudaProfilerStart/Stop,
+    for launch-list captures with ``ncu --profile-from-start off``:
+    ``python bench_solve.py --profile c3 1``."""
+    P = _mesh.config_mesh(cfg)
+    extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
+    S = DeviceSystem(Model(cfg, P, STEEL, extra_loads=extra))
+    S.amg()
+    F = S.F if nrhs == 1 else S.F.reshape(-1, 1).repeat(1, nrhs).contiguous()
+    S.solve(F=F, rtol=1e-10, mixed=False, precond="amg")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    U, st = S.solve(F=F, rtol=1e-10, mixed=False, precond="amg")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print({k: st[k] for k in ("status", "iterations", "relres", "time_ms")})
+
+
+if __name__ == "__main__":
+    import sys
+    if len(sys.argv) >= 2 and sys.argv[1] == "--profile":
+        profile_solve(sys.argv[2] if len(sys.argv) > 2 else "c3", int(sys.argv[3]) if len(sys.argv) > 3 else 1)

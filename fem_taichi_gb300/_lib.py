@@ -111,7 +111,6 @@ SIGNATURES = {
                                       c_size_t, c_void_p]),
     "fem_assemble_gather": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t,
                                     c_void_p]),
-    "fem_diag_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p]),
     "fem_assemble_host": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), ctypes.POINTER(FemAssemblyOut),
                                   c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_size_t, c_void_p]),

@@ -18,6 +18,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfemgb.so")
+# measurement-only library of the benchmark (arithmetic-rate probes), not part of the product
+PROBE_SRC = os.path.join(HERE, "probe", "fp64_rate.cu")
+PROBE_LIB = os.path.join(OUT, "libfemprobe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
@@ -53,6 +56,17 @@ def _compile(src: str, extra) -> str:
         cmd += ["-x", "cu"] if False else []
     subprocess.run(cmd, check=True)
     return obj
+
+
+def build_probe(force: bool = False) -> str:
+    """Compile the benchmark's rate probes into libfemprobe.so; returns its path."""
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= os.path.getmtime(PROBE_SRC):
+        return PROBE_LIB
+    os.makedirs(OUT, exist_ok=True)
+    tmp = PROBE_LIB + ".tmp"
+    subprocess.run([nvcc(), "-shared", "-o", tmp, PROBE_SRC, "-O3", "-Xcompiler", "-fPIC"] + ARCH, check=True)
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:

@@ -168,9 +168,9 @@ class Physics:
 # ---------------------------------------------------------------------------------------
 # Synthetic structured hexahedral blocks (seeded)
 # ---------------------------------------------------------------------------------------
-def hex_block(nx, ny, nz, size=None, jitter=0.0, seed=0, twist_deg=0.0, origin=(0.0, 0.0, 0.0),
-              center_yz=False, fix="zmin", load_face=None, load=(0.0, 0.0, 0.0), name="block"):
-    """Structured nx*ny*nz hex block with seeded interior-node jitter.
+def block_arrays(nx, ny, nz, size=None, jitter=0.0, seed=0, twist_deg=0.0, origin=(0.0, 0.0, 0.0),
+                 center_yz=False, fix="zmin", load_face=None, load=(0.0, 0.0, 0.0)):
+    """Arrays of a structured nx*ny*nz hex block with seeded interior-node jitter (numpy only).
 
     size: (Lx, Ly, Lz) extents (default one unit per element).  jitter: amplitude as a
     fraction of the element size in each direction, applied to nodes strictly inside the
@@ -178,6 +178,9 @@ def hex_block(nx, ny, nz, size=None, jitter=0.0, seed=0, twist_deg=0.0, origin=(
     axis (through the y-z centre) from 0 at x = 0 to twist_deg at x = Lx.  fix / load_face:
     face name ('xmin','xmax','ymin','ymax','zmin','zmax' or None) whose nodes go to Bounds
     (all DOFs) / Forces (value ``load``).  Node ids are 1-based, x fastest.
+
+    Returns a dict: ids (N,), xyz (N, 3), elem (8, E) node ids - 1, bounds, forces (the
+    reference's [ids - 1, [3 values]] groups), grid_index (ix, iy, iz), h.
     """
     size = size or (float(nx), float(ny), float(nz))
     h = np.array([size[0] / nx, size[1] / ny, size[2] / nz])
@@ -216,10 +219,19 @@ def hex_block(nx, ny, nz, size=None, jitter=0.0, seed=0, twist_deg=0.0, origin=(
 
     bounds = [[face(fix), [0, 0, 0]]] if fix else []
     forces = [[face(load_face), list(load)]] if load_face else []
-    P = Physics(ids, xyz, elem, bounds, forces, name=name)
+    return {"ids": ids, "xyz": xyz, "elem": elem, "bounds": bounds, "forces": forces,
+            "grid_index": (ix, iy, iz), "h": h}
+
+
+def hex_block(nx, ny, nz, size=None, jitter=0.0, seed=0, twist_deg=0.0, origin=(0.0, 0.0, 0.0),
+              center_yz=False, fix="zmin", load_face=None, load=(0.0, 0.0, 0.0), name="block"):
+    """Structured nx*ny*nz hex block (see ``block_arrays``) as a Physics object."""
+    b = block_arrays(nx, ny, nz, size=size, jitter=jitter, seed=seed, twist_deg=twist_deg, origin=origin,
+                     center_yz=center_yz, fix=fix, load_face=load_face, load=load)
+    P = Physics(b["ids"], b["xyz"], b["elem"], b["bounds"], b["forces"], name=name)
     P.grid = (nx, ny, nz)
-    P.grid_index = (ix, iy, iz)
-    P.h = h
+    P.grid_index = b["grid_index"]
+    P.h = b["h"]
     return P
 
 

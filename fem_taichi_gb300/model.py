@@ -110,7 +110,7 @@ class Model:
     """Drop-in GPU replacement of the reference FE model (linear part)."""
 
     def __init__(self, name, Physics, Materials, Omegas=(0, 0, 100), Largedisp=False, device="cuda",
-                 extra_loads=None, algo="dd"):
+                 extra_loads=None, algo="fp64"):
         self.name = name
         self.DE, self.EX, self.PO = Materials['DE'], Materials['EX'], Materials['PO']
         self.OM = np.array(Omegas, dtype=np.float64)
@@ -155,7 +155,8 @@ class Model:
 
         k_layout 'bsr' -> K (nnzb, 3, 3); 'csr' -> K (9*nnzb,) in the reference CSR order.
         m_layout 'bsr' -> M (nnzb,);       'csr' -> M (3*nnzb,) reference CSR order.
-        algo: 'dd' (double-float element integrals and sums, default) or 'fp64'.
+        algo: 'fp64' (FP64 arithmetic, default) or 'dd' (double-float pairs on the FP32 pipes,
+        about 48-bit significands).
         """
         algo = self.algo if algo is None else algo
         d = self.device

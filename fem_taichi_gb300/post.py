@@ -6,10 +6,15 @@ table [xx, yy, zz, xy, yz, xz, p1, p2, p3, VM] exactly as the reference lays it 
 
 Extrapolation table.  get_NdSol (POST_process.py:172-181) weights Gauss point k's stress
 for element corner j by shapefunc_GS(GMat[j])[k].  GMat is assigned eight corner points
-(POST_process.py:310-317) but declared with two entries (POST_process.py:145).
-``gmat_mode='written'`` (default) uses the eight assigned points; ``gmat_mode='aliased'``
-uses entry j & 1 holding the last value written to it, which is what a runtime that maps
-an out-of-range index of a 2-entry dense field onto its low bit would read.
+(POST_process.py:310-317) but declared with two entries (POST_process.py:145).  Taichi 0.6
+(the reference's pinned runtime) lowers a dense-field index to its low bits, without a bounds
+check, so entry j reads entry j & 1, which holds the last value written to it: (1, 1, -1) for
+even j and (1, 1, 1) for odd j.  ``gmat_mode='aliased'`` (default) is that reading, the one
+the reference's own code produces when executed; ``gmat_mode='written'`` uses the eight
+assigned points (what the source appears to intend).
+
+Arithmetic.  ``algo='fp64'`` (default) computes on the FP64 pipe; ``algo='dd'`` uses
+double-float pairs on the FP32 pipes (about 48-bit significands; faster, not FP64).
 """
 from __future__ import annotations
 
@@ -28,7 +33,7 @@ _GMAT_WRITTEN = np.array([[-1, -1, -1], [-1, -1, 1], [-1, 1, -1], [-1, 1, 1],
                           [1, -1, -1], [1, -1, 1], [1, 1, -1], [1, 1, 1]], dtype=np.float64)
 
 
-def extrapolation_table(gmat_mode: str = "written") -> np.ndarray:
+def extrapolation_table(gmat_mode: str = "aliased") -> np.ndarray:
     """W[j, k] = shapefunc_GS(GMat[j])[k] (POST_process.py:212-223)."""
     if gmat_mode == "written":
         g = _GMAT_WRITTEN
@@ -82,8 +87,8 @@ def write_tecplot_ascii(output_file, title, Physics, Fields, Field_names):
 class Post:
     """Drop-in for POST_process.Post (stress part)."""
 
-    def __init__(self, name, Physics, Materials, Solutions, gmat_mode="written", device="cuda", mesh=None,
-                 algo="dd"):
+    def __init__(self, name, Physics, Materials, Solutions, gmat_mode="aliased", device="cuda", mesh=None,
+                 algo="fp64"):
         self.name = name
         self.DE, self.EX, self.PO = Materials['DE'], Materials['EX'], Materials['PO']
         self.Physics = Physics

@@ -388,12 +388,6 @@ int fem_mlp_adam(float* params, const float* grad, float* m, float* v, int step,
 /* P[n][9] = G^{-T} C G^{-1} (FP64) from the MLP outputs. */
 int fem_learned_blocks(int64_t n, const float* out, const double* ginv, double* P, void* stream);
 
-/* ---- diagnostics ------------------------------------------------------------------ */
-/* Measured FP64 FMA throughput of this device (TFLOP/s, 2 flops per FMA), from a kernel of
- * independent fma chains timed with CUDA events on `stream`.  No reference counterpart: it
- * supplies the FP64 roofline denominator for the FP64-bound element kernels. */
-int fem_diag_fp64_tflops(double* tflops, void* stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,8 @@
  * With nthreads == 1 the scatter order is element-major (e, j, k), i.e. the order a
  * serial run of the reference kernels would use.
  *
- * PARITY UNPINNED: the reference has no golden vectors for this path and cannot run here.
+ * Parity: agrees with the numpy restatement (oracle/fem_oracle.py), which is pinned to
+ * outputs of the reference's own code (tests/golden/refexec_*.npz, tests/test_refexec.py).
  */
 #include <math.h>
 #include <stdint.h>

@@ -10,12 +10,18 @@ It is the checker against which the CUDA path is compared.  Nothing in the produ
 package imports it; only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
 CPU-baseline leg may use it.
 
-PARITY UNPINNED: the reference ships no golden vectors, known-answer tests or fixtures
-for this path (its only test file exercises a third-party Pardiso wrapper), and the
-reference itself cannot run here (its JIT, taichi 0.6.28, is not installed).  The
-restatement is instead cross-checked against (a) an independent C restatement
-(``fem_oracle.c``), and (b) analytic known-answer properties (rigid-body null space,
+PARITY PINNED to the reference's own execution: the reference ships no golden vectors for
+this path (its only test file exercises a third-party Pardiso wrapper) and its JIT (taichi
+0.6.28) is not installed, so its unmodified FEM_model_csr.py / FEM_model_bsr.py /
+POST_process.py were run under a pure-Python restatement of the Taichi constructs they use
+(``oracle/refexec``), producing ``tests/golden/refexec_*.npz``; this module agrees with
+those outputs (``tests/test_refexec.py``).  It is also cross-checked against an independent
+C restatement (``fem_oracle.c``) and analytic known-answer properties (rigid-body null space,
 symmetry, total mass, centrifugal resultant, constant-stress patch test).
+
+GMat reading: the reference's shape-2 GMat field read with indices 0..7 resolves, under
+Taichi 0.6's dense addressing, to entry j & 1 ('aliased', the default here); 'written'
+(the eight assigned corners) is kept for comparison.
 
 Every function cites the reference file:line it follows.
 """
@@ -101,7 +107,7 @@ def shapefunc_gs(rtr):
         0.125 * (1 + a) * (1 - b) * (1 + c)], dtype=np.float64)
 
 
-def extrapolation_table(gmat_mode: str = "written") -> np.ndarray:
+def extrapolation_table(gmat_mode: str = "aliased") -> np.ndarray:
     """W[j, k]: weight of GP k's stress in node j's value (POST_process.py:176-181)."""
     g = GMAT_WRITTEN if gmat_mode == "written" else GMAT_ALIASED
     return np.stack([shapefunc_gs(g[j]) for j in range(8)])
@@ -474,7 +480,7 @@ def csr_direct_K(Physics, ValKT):
 # ---------------------------------------------------------------------------
 # Stress recovery: POST_process.py
 # ---------------------------------------------------------------------------
-def oracle_stress(Physics, Materials, Solutions, gmat_mode="written", chunk=4096):
+def oracle_stress(Physics, Materials, Solutions, gmat_mode="aliased", chunk=4096):
     """Post.Get_Stress (POST_process.py:72-99) with get_NdSol :172-181, get_NdAve :183-187,
     UnitVectorS :190-209 (B2 rows xy, yz, xz) and shapefunc_GS :212-223.
 

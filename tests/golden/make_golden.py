@@ -10,7 +10,7 @@ mesh2_golden.npz -- oracle outputs on that mesh (steel, Omegas=(0,0,100), both b
                     and of the stress table for a seeded displacement field.  They pin
                     the oracle across machines; the reference itself cannot run here.
 
-Usage:  python tests/golden/make_golden.py [reference_root]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
 """
 from __future__ import annotations
 
@@ -49,7 +49,7 @@ def parse_lis_like_reference(path):
     return np.array(" ".join(keep).split(), dtype=np.int64)
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root):
     Node, Elem = parse_cdb_like_reference(os.path.join(ref_root, "Mesh", "2.cdb"))
     bot_in = parse_lis_like_reference(os.path.join(ref_root, "Boundary", "2_bot_in.lis"))
     bot_out = parse_lis_like_reference(os.path.join(ref_root, "Boundary", "2_bot_out.lis"))
@@ -89,4 +89,6 @@ def main(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT")
+    main(sys.argv[1])

@@ -74,3 +74,6 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    # the reference arm times the full workload mesh and never maps the product library
+    assert d["config"]["same_config"] is True and "19,200 elements" in d["config"]["workload"]
+    assert all(p.startswith("oracle/") for p in d["native_so_loaded"]), d["native_so_loaded"]
