@@ -499,8 +499,8 @@ def main():
         import bench_solve as study
 
         def brief(r):
-            keep = ("label", "wall_s", "iterations", "outer", "relres", "floor", "relerr", "meets_1e-8", "status_text",
-                    "ms_per_iteration", "nrhs", "setup_s")
+            keep = ("label", "wall_s", "iterations", "outer", "rtol", "relres", "floor", "at_floor", "relerr",
+                    "meets_1e-8", "status_text", "ms_per_iteration", "nrhs", "setup_s")
             out = {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
             if "amg" in r:
                 out["amg_setup"] = r["amg"]

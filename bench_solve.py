@@ -82,14 +82,29 @@ def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda"):
                  "loss_end": hist[-1], "data_s": t_data, "train_s": t_train}
 
 
-def reference_solution(S: DeviceSystem, F=None, precond=None, mixed=True, rtol=(1e-13, 1e-12)):
-    """FP64 reference (to rtol[0]) and its relative difference from a solve to rtol[1]."""
-    kw = dict(F=F, mixed=mixed, maxit=200000, inner_maxit=50000, max_outer=60, precond=precond)
-    U1, s1 = S.solve(rtol=rtol[0], **kw)
-    U2, s2 = S.solve(rtol=rtol[1], **kw)
-    est = float(torch.linalg.norm(U1 - U2) / torch.linalg.norm(U1))
-    return U1, {"relres": s1["relres"], "status": s1["status"], f"est_err_of_{rtol[1]:g}_solve": est,
-                "precond": precond or "block Jacobi", "mixed": s1["mixed"], "iterations": s1["iterations"]}
+def reference_solution(S: DeviceSystem, F=None, precond="amg", check=None, check_cols=None, check_name=None):
+    """FP64 reference solution standing in for the reference's Pardiso (SOLVE_static.py:31-33):
+    FP64 PCG followed by residual-replacement refinement on compensated (twice-FP64-accurate)
+    residuals, until the true residual stops falling -- the FP64 floor of the system, where
+    U is as accurate as FP64 storage allows.  Its forward error is estimated by the relative
+    difference to a second reference computed the same way with another preconditioner
+    ``check`` (block Jacobi when None; on the columns ``check_cols`` of F when given)."""
+    kw = dict(mixed=False, maxit=400000, max_outer=10, residual="extra", rtol=1e-15)
+    t = time.perf_counter()
+    U1, s1 = S.solve(F=F, precond=precond, **kw)
+    torch.cuda.synchronize()
+    out = {"method": "FP64 PCG (%s) + refinement on compensated residuals, to the FP64 floor"
+                     % ("multigrid" if precond is not None else "block Jacobi"),
+           "relres": s1["relres"], "floor": s1["floor"], "status_text": s1["status_text"],
+           "iterations": s1["iterations"], "outer": s1["outer"], "wall_s": time.perf_counter() - t}
+    Fc = F if (F is None or check_cols is None) else F[:, check_cols].contiguous()
+    U2, s2 = S.solve(F=Fc, precond=check, **kw)
+    U1c = U1 if check_cols is None else U1[:, check_cols]
+    out["check"] = {"precond": check_name or ("block Jacobi" if check is None else "multigrid"),
+                    "relres": s2["relres"], "floor": s2["floor"], "iterations": s2["iterations"],
+                    "columns": "all" if check_cols is None else list(check_cols)}
+    out["est_err"] = relerr(U2, U1c)
+    return U1, out
 
 
 def amg_setup(S: DeviceSystem, **opts):
@@ -126,13 +141,21 @@ def timed_solve(S, label, reps=1, **kw):
     return U, st
 
 
-def compare(S: DeviceSystem, Ur, variants, F=None, target=1e-8):
-    """Each variant: (label, kwargs).  Adds relative error vs Ur; marks pass at target."""
+def compare(S: DeviceSystem, Ur, variants, F=None, target=1e-8, amg=None):
+    """Each variant: (label, kwargs).  Adds the relative error vs Ur and whether it meets the
+    error target; multigrid rows carry the hierarchy's setup time (``setup_s``, not in
+    wall_s).  ``status_text`` is the solver's own verdict on its true residual: "converged"
+    only when it is <= rtol; "not converged" rows show where they stopped (``relres``) and
+    the FP64 floor of the system (``floor``)."""
     rows = []
     for label, kw in variants:
         U, st = timed_solve(S, label, F=F, **kw)
         st["relerr"] = relerr(U, Ur)
-        st["meets_1e-8"] = bool(st["relerr"] <= target and st["status"] == 0)
+        st["rtol"] = kw.get("rtol")
+        st["at_floor"] = bool(st["relres"] <= 16 * st["floor"])
+        st["meets_1e-8"] = bool(st["relerr"] <= target)
+        if amg is not None and (kw.get("precond") == "amg"):
+            st["setup_s"] = amg["wall_s"]
         rows.append(st)
     return rows
 
@@ -193,19 +216,38 @@ def c3_study(device="cuda", rtol=1e-10, peak_gbs=None):
     P = _mesh.config_mesh("c3")
     extra = _mesh.face_traction_loads(P, "zmax", (0.0, 0.0, -1.0))
     S = DeviceSystem(Model("c3", P, STEEL, device=device, extra_loads=extra))
-    Ur, ref = reference_solution(S)
     amg = amg_setup(S)
+    Ur, ref = reference_solution(S)
     rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
                            ("mixed_bj", dict(rtol=rtol, mixed=True)),
                            ("mixed_amg", dict(rtol=rtol, mixed=True, precond="amg")),
-                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))])
+                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))], amg=amg)
     for r in rows:
         r["ms_per_iteration"] = 1e3 * r["wall_s"] / max(r["iterations"], 1)
     return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows,
             "amg": amg, "spmv": spmv_rates(S, peak_gbs=peak_gbs)}
 
 
-def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
+def face_rhs(S: DeviceSystem, P, F0, nrhs, face, seed):
+    """nrhs right-hand sides: F0 and nrhs - 1 seeded random nodal loads N(0, 1) N on a face."""
+    nx, ny, nz = P.grid
+    ix, iy, iz = P.grid_index
+    sel = {"xmax": ix == nx, "zmax": iz == nz}[face]
+    nodes = np.nonzero(sel)[0]
+    rng = np.random.default_rng(seed)
+    Fm = torch.zeros((3 * P.Num_Node, nrhs), dtype=torch.float64, device=S.device)
+    Fm[:, 0] = F0
+    for k in range(1, nrhs):
+        f = np.zeros((P.Num_Node, 3))
+        f[nodes] = rng.standard_normal((nodes.size, 3))
+        Fm[:, k] = torch.from_numpy(f.reshape(-1)).to(S.device)
+    return Fm
+
+
+def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32):
+    """Learned preconditioner on the unseen 160x160x20 block: 1 and 32 right-hand sides
+    (the top traction plus 31 seeded random top-face loads), learned vs plain block Jacobi,
+    against the FP64 reference."""
     info = {}
     if net is None:
         net, info = train_c4(device=device, **(train_kw or {}))
@@ -217,54 +259,66 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None):
     Pl = net.blocks(S)
     torch.cuda.synchronize()
     t_inf = time.perf_counter() - t
-    Ur, ref = reference_solution(S)
     amg = amg_setup(S)
+    Fm = face_rhs(S, P, S.F, nrhs, "zmax", seed=4)
+    Urm, ref = reference_solution(S, F=Fm, check_cols=[0, 1, 2, 3])
+    Ur = Urm[:, 0].contiguous()
+    F1 = Fm[:, 0].contiguous()
     rows = compare(S, Ur, [("fp64_bj", dict(rtol=rtol, mixed=False)),
                            ("mixed_bj", dict(rtol=rtol, mixed=True)),
                            ("mixed_learned", dict(rtol=rtol, mixed=True, precond=Pl)),
                            ("fp64_learned", dict(rtol=rtol, mixed=False, precond=Pl)),
                            ("mixed_amg", dict(rtol=rtol, mixed=True, precond="amg")),
-                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))])
-    return {"workload": "c4 eval 160x160x20, 544,341 nodes", "training": info, "inference_s": t_inf,
-            "reference": ref, "solves": rows, "amg": amg}, net
+                           ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))], F=F1, amg=amg)
+    rows += compare(S, Urm, [("fp64_bj_32rhs", dict(rtol=rtol, mixed=False)),
+                             ("mixed_bj_32rhs", dict(rtol=rtol, mixed=True)),
+                             ("mixed_learned_32rhs", dict(rtol=rtol, mixed=True, precond=Pl)),
+                             ("fp64_amg_32rhs", dict(rtol=rtol, mixed=False, precond="amg"))], F=Fm, amg=amg)
+    by = {r["label"]: r for r in rows}
+    gain = {}
+    for suffix in ("", "_32rhs"):
+        lb, bj, fb = by["mixed_learned" + suffix], by["mixed_bj" + suffix], by["fp64_bj" + suffix]
+        gain["learned_vs_mixed_bj" + suffix] = {"iterations": lb["iterations"] / max(bj["iterations"], 1),
+                                               "wall": lb["wall_s"] / bj["wall_s"]}
+        gain["learned_mixed_vs_fp64_bj" + suffix] = {"wall": lb["wall_s"] / fb["wall_s"]}
+    return {"workload": "c4 eval 160x160x20, 544,341 nodes, 1 and %d RHS" % nrhs, "training": info,
+            "inference_s": t_inf, "reference": ref, "solves": rows, "amg": amg, "gain": gain}, net
 
 
 def c5_system(device="cuda", nrhs=32, seed=5):
     P = _mesh.config_mesh("c5")
     M = Model("c5", P, STEEL, device=device)
     S = DeviceSystem(M)
-    nx, ny, nz = P.grid
-    ix, iy, iz = P.grid_index
-    tip = np.nonzero(ix == nx)[0]
-    rng = np.random.default_rng(seed)
-    Fm = torch.zeros((3 * P.Num_Node, nrhs), dtype=torch.float64, device=S.device)
-    Fm[:, 0] = S.F
-    for k in range(1, nrhs):
-        f = np.zeros((P.Num_Node, 3))
-        f[tip] = rng.standard_normal((tip.size, 3))
-        Fm[:, k] = torch.from_numpy(f.reshape(-1)).to(S.device)
-    return S, Fm
+    return S, face_rhs(S, P, S.F, nrhs, "xmax", seed)
 
 
-def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=3000, block_variants=True):
+def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=1000, block_variants=True):
     """32 right-hand sides on the slender twisted slab (condition number far beyond FP32
-    refinement).  The reference solve and the ``fp64_amg`` rows run FP64 flexible CG around
-    the FP32 multigrid cycle; block-diagonal preconditioners (capped at ``maxit`` iterations)
-    do not reach 1e-8 here and are reported with the error they reach."""
+    refinement).  The reference is the FP64 multigrid solve refined on compensated residuals
+    to the FP64 floor, cross-checked on 4 columns by the same procedure with a differently
+    built hierarchy (theta 0.16, degree-3 Chebyshev).  Block-diagonal preconditioners are run
+    on the first right-hand side with an iteration cap and reported with the error they
+    reach ("not converged in `maxit` iterations")."""
     S, Fm = c5_system(device, nrhs)
     amg = amg_setup(S)
-    Ur, ref = reference_solution(S, F=Fm, precond="amg", mixed=False, rtol=(1e-12, 1e-11))
+    H2 = S.amg_variant(theta=0.16, pre_degree=3, post_degree=3)
+    Ur, ref = reference_solution(S, F=Fm, precond="amg", check=H2, check_cols=[0, 1, 2, 3],
+                                 check_name="multigrid, theta 0.16, degree-3 Chebyshev")
+    H2.close()
     variants = [("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg")),
+                ("fp64_amg_extra_residual", dict(rtol=rtol, mixed=False, precond="amg", residual="extra")),
                 ("fp64_amg_1rhs", dict(F=Fm[:, 0].contiguous(), rtol=rtol, mixed=False, precond="amg"))]
     rows = []
     for label, kw in variants:
         F_ = kw.pop("F", Fm)
         U, st = timed_solve(S, label, F=F_, **kw)
         st["relerr"] = relerr(U, Ur if F_.dim() == 2 else Ur[:, 0])
-        st["meets_1e-8"] = bool(st["relerr"] <= 1e-8 and st["status"] == 0)
+        st["rtol"] = rtol
+        st["at_floor"] = bool(st["relres"] <= 16 * st["floor"])
+        st["meets_1e-8"] = bool(st["relerr"] <= 1e-8)
+        st["setup_s"] = amg["wall_s"]
         rows.append(st)
     if block_variants:
-        # block-diagonal preconditioners on the first right-hand side, capped at maxit
         F1, U1r = Fm[:, 0].contiguous(), Ur[:, 0].contiguous()
         bv = [("fp64_bj_1rhs_capped", dict(rtol=rtol, mixed=False, maxit=maxit))]
         if net is not None:
@@ -295,6 +349,7 @@ def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda", precond="a
     return {"workload": f"{cfg}: {P.Num_Node:,} nodes, {num_eigen} modes, block {num_block}", "precond": precond,
             "wall_s": wall,
             "steps": solver.last_stats["steps"], "solve_iterations": solver.last_stats["solve_iterations"],
+            "phase_ms": solver.last_stats["phase_ms"],
             "lowest_freq_hz": [float(f) for f in freq[:5]], "M_orthonormality_err": orth}
 
 

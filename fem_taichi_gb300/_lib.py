@@ -26,6 +26,8 @@ FEM_ERR_MAXITER = -5
 FEM_ERR_NOT_SPD = -6
 FEM_ERR_WORKSPACE = -7
 FEM_ERR_BREAKDOWN = -8
+RESIDUAL_FP64 = 0
+RESIDUAL_EXTRA = 1
 
 LAYOUT_BSR = 0
 LAYOUT_CSR = 1
@@ -71,12 +73,12 @@ class FemBsr(ctypes.Structure):
 class FemPcgOpts(ctypes.Structure):
     _fields_ = [("nrhs", c_int), ("mixed", c_int), ("rtol", c_double), ("maxit", c_int), ("inner_rtol", c_double),
                 ("inner_maxit", c_int), ("max_outer", c_int), ("use_graph", c_int), ("unroll", c_int),
-                ("spmv_variant", c_int), ("spmv_variant32", c_int)]
+                ("spmv_variant", c_int), ("spmv_variant32", c_int), ("residual", c_int), ("stall_window", c_int)]
 
 
 class FemPcgStats(ctypes.Structure):
     _fields_ = [("status", c_int), ("iterations", c_int), ("outer", c_int), ("relres", c_double),
-                ("time_ms", c_double)]
+                ("time_ms", c_double), ("floor", c_double)]
 
 
 class FemAmgOpts(ctypes.Structure):

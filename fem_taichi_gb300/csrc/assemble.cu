@@ -21,6 +21,7 @@
 //     reproducible bit for bit.  The penalty (FEM_model_bsr.py:248-259) and nodal loads
 //     (LoadF, :220-226) are applied in the same pass, and the row is written in either
 //     the BSR block order or the reference's scalar-CSR order (FEM_model_csr.py:150-173).
+#include <climits>
 #include <vector>
 
 #include "fem_common.cuh"
@@ -38,16 +39,18 @@ constexpr int kRPad = 25;                // padded row (24 used) to spread smem 
 struct ElemParams {
     const double* xyz;
     const int4* conn4;
-    int64_t n_elem;
+    int64_t e_begin, e_end;  // elements [e_begin, e_end) of this launch
     double* rec;
     double DE, D0d, lam, mu;
     double w0, w1, w2;
     DevTables tab;
+    double nn[36][8];  // N_a(g) N_b(g) for pair (a <= b), Gauss point g
 };
 
 struct ElemSmem {
     double dnr[8][8][3];
     double nr[8][8];
+    double nn[36][8];
     double x[kEpc][8][3];
     double R[kEpc][8][kRPad];   // R_a(g)[i] at [el][g][3a+i]
     double Rs[kEpc][8][kRPad];  // R_a(g)[i] / det_g
@@ -73,11 +76,12 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
     const int tid = threadIdx.x;
     const int el = tid >> 3;
     const int t = tid & 7;
-    const int64_t e = int64_t(blockIdx.x) * kEpc + el;
-    const bool valid = e < p.n_elem;
+    const int64_t e = p.e_begin + int64_t(blockIdx.x) * kEpc + el;
+    const bool valid = e < p.e_end;
 
     for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
     for (int k = tid; k < 64; k += kElemThreads) (&s.nr[0][0])[k] = (&p.tab.nr[0][0])[k];
+    for (int k = tid; k < 36 * 8; k += kElemThreads) (&s.nn[0][0])[k] = (&p.nn[0][0])[k];
     if (valid) {
         const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
         const int node = __ldg(cn + t);
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
     const double lam = p.lam, mu = p.mu, D0d = p.D0d, DE = p.DE;
     // diagonal pair (t, t): P symmetric
     {
-        const int a = t;
+        const int a = t, pi = pair_index(a, a);
         double P00 = 0, P11 = 0, P22 = 0, P01 = 0, P02 = 0, P12 = 0, m = 0;
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
@@ -156,10 +160,10 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
             P01 = fma(q0, r1, P01);
             P02 = fma(q0, r2, P02);
             P12 = fma(q1, r2, P12);
-            m = fma(s.det[el][g], s.nr[g][a] * s.nr[g][a], m);
+            m = fma(s.det[el][g], s.nn[pi][g], m);
         }
         const double lm = lam + mu;
-        double* o = rec + pair_index(a, a) * kPairStride;
+        double* o = rec + pi * kPairStride;
         o[0] = D0d * P00 + mu * (P11 + P22);
         o[4] = D0d * P11 + mu * (P00 + P22);
         o[8] = D0d * P22 + mu * (P00 + P11);
@@ -172,6 +176,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
     for (int q = t; q < 28; q += 8) {
         int a, b;
         offdiag_pair(q, a, b);
+        const int pi = pair_index(a, b);
         double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         double m = 0;
 #pragma unroll
@@ -187,9 +192,9 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
             P[2][0] = fma(q2, r0, P[2][0]);
             P[2][1] = fma(q2, r1, P[2][1]);
             P[2][2] = fma(q2, r2, P[2][2]);
-            m = fma(s.det[el][g], s.nr[g][a] * s.nr[g][b], m);
+            m = fma(s.det[el][g], s.nn[pi][g], m);
         }
-        double* o = rec + pair_index(a, b) * kPairStride;
+        double* o = rec + pi * kPairStride;
         o[0] = D0d * P[0][0] + mu * (P[1][1] + P[2][2]);
         o[4] = D0d * P[1][1] + mu * (P[0][0] + P[2][2]);
         o[8] = D0d * P[2][2] + mu * (P[0][0] + P[1][1]);
@@ -324,6 +329,264 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams p) {
     }
 }
 
+// ---- FP64 gather, lane = (row, element corner) -------------------------------------------------
+//
+// One warp per 4 block rows; lane (r, b) handles corner b of every element incident to row r.
+// For incident entry k (ascending element index) it reads the element block of the pair
+// (a, b) -- a = the row's corner in that element -- from the element record (transposed when
+// a > b) and adds it into the row's shared-memory accumulator at the slot given by the
+// element-to-block map (slot_map).  All 8 lanes of a row do useful FP64 work on every entry.
+// The first contribution to a slot is stored instead of added (a per-row bit mask of the
+// slots already holding a value), which saves the ~27 of ~64 block additions per interior
+// row that would add into zero.  A repeated corner node of a degenerate element adds after
+// the earlier corner.  The summation order (element by element, corners ascending) is fixed,
+// so results are bitwise reproducible.  Rows with more than kG64MaxL blocks use the
+// lane-per-slot path (same order).
+constexpr int kG64Warps = 4;
+constexpr int kG64Rows = 4;
+constexpr int kG64MaxL = 32;
+constexpr int kG64RowStride = kG64MaxL * kPairStride + 4;  // +4 doubles: rows start 8 banks apart
+
+struct Gather64Params {
+    int64_t row_begin, row_end;  // block rows [row_begin, row_end) of this launch
+    const int32_t* indptr;
+    const int32_t* indices;
+    const int32_t* ne_ptr;
+    const int32_t* ne_list;
+    const uint8_t* slot_map;
+    const int4* conn4;
+    const double* rec;
+    int k_layout, m_layout;
+    double* K;
+    double* M;
+    double* F;
+    const uint8_t* fixed;
+    const double* loads;
+};
+
+struct Gather64Smem {
+    double acc[kG64Warps][kG64Rows][kG64RowStride];
+    int cols[kG64Warps][kG64Rows][kG64MaxL];
+};
+
+// Block (a, b) of element e as 10 doubles (K row-major, then M); the record stores a <= b.
+__device__ __forceinline__ void load_pair_block(const double* rec, int64_t e, int a, int b, double (&v)[kPairStride]) {
+    const int lo = min(a, b), hi = max(a, b);
+    const double2* blk = reinterpret_cast<const double2*>(rec + e * kRec + pair_index(lo, hi) * kPairStride);
+    double w[kPairStride];
+#pragma unroll
+    for (int q = 0; q < kPairStride / 2; ++q) {
+        const double2 x = __ldg(blk + q);
+        w[2 * q] = x.x;
+        w[2 * q + 1] = x.y;
+    }
+    const bool tr = a > b;
+#pragma unroll
+    for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq) v[3 * pp + qq] = tr ? w[3 * qq + pp] : w[3 * pp + qq];
+    v[9] = w[9];
+}
+
+__device__ __forceinline__ int find_slot64(const int* cols, int L, int node) {
+    int lo = 0, hi = L - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cols[mid] < node) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Lane-per-slot path for one row of any length (K and M; F is summed by the caller).
+__device__ void gather_row_long64(const Gather64Params& p, int64_t row, int lane) {
+    const int64_t rs = p.indptr[row];
+    const int L = p.indptr[row + 1] - int(rs);
+    const int ks = p.ne_ptr[row], ke = p.ne_ptr[row + 1];
+    const unsigned fixed_bits = p.fixed ? p.fixed[row] : 0u;
+    for (int base = 0; base < L; base += 32) {
+        const int l = base + lane;
+        const bool active = l < L;
+        double acc[kPairStride];
+#pragma unroll
+        for (int q = 0; q < kPairStride; ++q) acc[q] = 0.0;
+        bool any = false;
+        for (int k = ks; k < ke; ++k) {
+            const int ent = __ldg(p.ne_list + k);
+            for (int b = 0; b < 8; ++b) {
+                if (int(__ldg(p.slot_map + 8 * int64_t(k) + b)) != l) continue;
+                double v[kPairStride];
+                load_pair_block(p.rec, ent >> 3, ent & 7, b, v);
+#pragma unroll
+                for (int q = 0; q < kPairStride; ++q) acc[q] = any ? acc[q] + v[q] : v[q];
+                any = true;
+            }
+        }
+        if (!active) continue;
+        const bool diag = __ldg(p.indices + rs + l) == int(row);
+        if (diag) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if ((fixed_bits >> d) & 1u) acc[4 * d] = 1e20;
+        }
+        if (p.K) {
+            if (p.k_layout == FEM_LAYOUT_BSR) {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) p.K[9 * (rs + l) + q] = acc[q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) p.K[9 * rs + int64_t(3 * (q / 3)) * L + 3 * l + (q % 3)] = acc[q];
+            }
+        }
+        if (p.M) {
+            if (p.m_layout == FEM_LAYOUT_BSR) p.M[rs + l] = acc[9];
+            else
+                for (int pp = 0; pp < 3; ++pp) p.M[3 * rs + int64_t(pp) * L + l] = acc[9];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kG64Warps * 32) k_gather64(const Gather64Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Gather64Smem& S = *reinterpret_cast<Gather64Smem*>(smem_raw);
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = lane >> 3, b = lane & 7;
+    const int64_t row0 = p.row_begin + (int64_t(blockIdx.x) * kG64Warps + w) * kG64Rows;
+    if (row0 >= p.row_end) return;  // uniform per warp
+    const int64_t row = row0 + r;
+    const bool vrow = row < p.row_end;
+    const int64_t rs = vrow ? p.indptr[row] : 0;
+    const int L = vrow ? p.indptr[row + 1] - int(rs) : 0;
+    const int ks = vrow ? p.ne_ptr[row] : 0;
+    const int cnt = vrow ? p.ne_ptr[row + 1] - ks : 0;
+
+    // ---- F of this row (lanes b < 3): corner loads in element order + nodal loads ----------
+    if (p.F && vrow && b < 3) {
+        double f = 0.0;
+        for (int k = 0; k < cnt; ++k) {
+            const int ent = __ldg(p.ne_list + ks + k);
+            f += __ldg(p.rec + int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b);
+        }
+        if (p.loads) f += p.loads[3 * row + b];
+        p.F[3 * row + b] = f;
+    }
+    if (!p.K && !p.M) return;
+
+    if (__any_sync(full, L > kG64MaxL)) {
+        for (int rr = 0; rr < kG64Rows; ++rr)
+            if (row0 + rr < p.row_end) gather_row_long64(p, row0 + rr, lane);
+        return;
+    }
+
+    int* cols = S.cols[w][r];
+    for (int l = b; l < kG64MaxL; l += 8) cols[l] = l < L ? __ldg(p.indices + rs + l) : INT_MAX;
+    double* accr = S.acc[w][r];
+
+    int maxcnt = cnt;
+#pragma unroll
+    for (int off = 8; off < 32; off <<= 1) maxcnt = max(maxcnt, __shfl_xor_sync(full, maxcnt, off));
+    unsigned touched = 0;  // slots of row r holding a value (the same in the row's 8 lanes)
+    double cur[kPairStride], nxt[kPairStride];
+    int cur_slot = 0, nxt_slot = 0;
+    if (cnt > 0) {
+        const int ent = __ldg(p.ne_list + ks);
+        load_pair_block(p.rec, ent >> 3, ent & 7, b, cur);
+        cur_slot = __ldg(p.slot_map + 8 * int64_t(ks) + b);
+    }
+    for (int k = 0; k < maxcnt; ++k) {
+        const bool active = k < cnt;
+        if (k + 1 < cnt) {
+            const int ent = __ldg(p.ne_list + ks + k + 1);
+            load_pair_block(p.rec, ent >> 3, ent & 7, b, nxt);
+            nxt_slot = __ldg(p.slot_map + 8 * int64_t(ks + k + 1) + b);
+        }
+        // a repeated corner node (degenerate element) maps two corners to one slot
+        bool dup = false;
+#pragma unroll
+        for (int bp = 0; bp < 7; ++bp) {
+            const int other = __shfl_sync(full, cur_slot, (lane & ~7) | bp);
+            if (bp < b && other == cur_slot) dup = true;
+        }
+        const unsigned bit = 1u << cur_slot;
+        double* a = accr + cur_slot * kPairStride;
+        if (active && !dup) {
+            if (touched & bit) {
+#pragma unroll
+                for (int q = 0; q < kPairStride; ++q) a[q] += cur[q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < kPairStride; ++q) a[q] = cur[q];
+            }
+        }
+        if (__any_sync(full, active && dup)) {
+            for (int bb = 1; bb < 8; ++bb) {
+                __syncwarp();
+                if (active && dup && b == bb) {
+#pragma unroll
+                    for (int q = 0; q < kPairStride; ++q) a[q] += cur[q];
+                }
+            }
+        }
+        unsigned nb = active ? bit : 0u;
+        nb |= __shfl_xor_sync(full, nb, 1);
+        nb |= __shfl_xor_sync(full, nb, 2);
+        nb |= __shfl_xor_sync(full, nb, 4);
+        touched |= nb;
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kPairStride; ++q) cur[q] = nxt[q];
+        cur_slot = nxt_slot;
+    }
+    __syncwarp();
+
+    // ---- write the four rows (all lanes, coalesced) -----------------------------------------
+    for (int rr = 0; rr < kG64Rows; ++rr) {
+        const int64_t rw = row0 + rr;
+        if (rw >= p.row_end) break;
+        const int64_t rrs = __shfl_sync(full, rs, rr * 8);
+        const int LL = __shfl_sync(full, L, rr * 8);
+        const unsigned tch = __shfl_sync(full, touched, rr * 8);
+        const unsigned fixed_bits = p.fixed ? p.fixed[rw] : 0u;
+        const int* cc = S.cols[w][rr];
+        const int sd = LL > 0 ? find_slot64(cc, LL, int(rw)) : 0;
+        const bool has_diag = LL > 0 && cc[sd] == int(rw);
+        const double* acc = S.acc[w][rr];
+        auto value = [&](int s_, int q) -> double {
+            if (!((tch >> s_) & 1u)) return 0.0;
+            double v = acc[s_ * kPairStride + q];
+            if (q < 9 && has_diag && s_ == sd && (q % 4 == 0) && ((fixed_bits >> (q / 4)) & 1u)) v = 1e20;
+            return v;
+        };
+        if (p.K) {
+            if (p.k_layout == FEM_LAYOUT_BSR) {
+                for (int o = lane; o < 9 * LL; o += 32) {
+                    const int s_ = o / 9;
+                    p.K[9 * rrs + o] = value(s_, o - 9 * s_);
+                }
+            } else {
+                for (int pp = 0; pp < 3; ++pp)
+                    for (int idx = lane; idx < 3 * LL; idx += 32) {
+                        const int s_ = idx / 3;
+                        p.K[9 * rrs + int64_t(3 * LL) * pp + idx] = value(s_, 3 * pp + (idx - 3 * s_));
+                    }
+            }
+        }
+        if (p.M) {
+            if (p.m_layout == FEM_LAYOUT_BSR) {
+                for (int o = lane; o < LL; o += 32) p.M[rrs + o] = value(o, 9);
+            } else {
+                for (int o = lane; o < LL; o += 32) {
+                    const double mv = value(o, 9);
+                    p.M[3 * rrs + o] = mv;
+                    p.M[3 * rrs + LL + o] = mv;
+                    p.M[3 * rrs + 2 * LL + o] = mv;
+                }
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_csr_index(int64_t n_node, const int32_t* __restrict__ indptr,
                                                    const int32_t* __restrict__ indices, int32_t* rowK,
                                                    int32_t* colK, int32_t* rowM, int32_t* colM) {
@@ -403,19 +666,17 @@ int launch_gather_dd(const fem_mesh* mesh, const fem_assembly_out* out, const vo
                      int64_t row_begin, int64_t row_end);
 }  // namespace fem
 
-extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int algo, void* workspace,
-                                     size_t workspace_bytes, void* stream) {
-    int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
-    if (rc) return rc;
-    FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
-    if (mesh->n_elem == 0) return FEM_OK;
-    FEM_REQUIRE(algo != FEM_ALGO_DD || (mesh->ne_inv && mesh->slot_map),
-                "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
-    if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream), 0, mesh->n_elem);
+namespace fem {
+namespace {
+
+int launch_hex8_element(const fem_mesh* mesh, const fem_material* mat, void* workspace, cudaStream_t st,
+                        int64_t e_begin, int64_t e_end) {
+    if (e_end <= e_begin) return FEM_OK;
     ElemParams ep;
     ep.xyz = mesh->xyz;
     ep.conn4 = reinterpret_cast<const int4*>(mesh->conn);
-    ep.n_elem = mesh->n_elem;
+    ep.e_begin = e_begin;
+    ep.e_end = e_end;
     ep.rec = static_cast<double*>(workspace);
     const double EX = mat->EX, PO = mat->PO;
     ep.DE = mat->DE;
@@ -426,12 +687,84 @@ extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* m
     ep.w1 = mat->omega[1];
     ep.w2 = mat->omega[2];
     ep.tab = make_tables();
+    const ShapeTables& T = shape_tables();
+    for (int a = 0; a < 8; ++a)
+        for (int b = a; b < 8; ++b)
+            for (int g = 0; g < 8; ++g) ep.nn[pair_index(a, b)][g] = T.nr[g][a] * T.nr[g][b];
     const size_t smem = sizeof(ElemSmem);
     FEM_CUDA(cudaFuncSetAttribute(k_hex8_element, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
-    k_hex8_element<<<unsigned(blocks), kElemThreads, smem, as_stream(stream)>>>(ep);
+    const int64_t blocks = (e_end - e_begin + kEpc - 1) / kEpc;
+    k_hex8_element<<<unsigned(blocks), kElemThreads, smem, st>>>(ep);
     FEM_LAUNCH_CHECK("k_hex8_element");
     return FEM_OK;
+}
+
+// FP64 gather of block rows [row_begin, row_end); the lane-per-corner kernel needs the
+// element-to-block map, the lane-per-slot kernel (whole mesh only) does not.
+int launch_gather64(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace, cudaStream_t st,
+                    int64_t row_begin, int64_t row_end) {
+    if (row_end <= row_begin) return FEM_OK;
+    if (!mesh->slot_map) {
+        FEM_REQUIRE(row_begin == 0 && row_end == mesh->n_node, "a partial FP64 gather needs mesh->slot_map");
+        GatherParams gp;
+        gp.n_node = mesh->n_node;
+        gp.indptr = mesh->indptr;
+        gp.indices = mesh->indices;
+        gp.ne_ptr = mesh->ne_ptr;
+        gp.ne_list = mesh->ne_list;
+        gp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+        gp.rec = static_cast<const double*>(workspace);
+        gp.k_layout = out->k_layout;
+        gp.m_layout = out->m_layout;
+        gp.K = out->K;
+        gp.M = out->M;
+        gp.F = out->F;
+        gp.fixed = out->fixed;
+        gp.loads = out->loads;
+        const int64_t blocks = (mesh->n_node * 32 + 255) / 256;
+        k_gather<<<unsigned(blocks), 256, 0, st>>>(gp);
+        FEM_LAUNCH_CHECK("k_gather");
+        return FEM_OK;
+    }
+    Gather64Params gp;
+    gp.row_begin = row_begin;
+    gp.row_end = row_end;
+    gp.indptr = mesh->indptr;
+    gp.indices = mesh->indices;
+    gp.ne_ptr = mesh->ne_ptr;
+    gp.ne_list = mesh->ne_list;
+    gp.slot_map = mesh->slot_map;
+    gp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
+    gp.rec = static_cast<const double*>(workspace);
+    gp.k_layout = out->k_layout;
+    gp.m_layout = out->m_layout;
+    gp.K = out->K;
+    gp.M = out->M;
+    gp.F = out->F;
+    gp.fixed = out->fixed;
+    gp.loads = out->loads;
+    const size_t smem = sizeof(Gather64Smem);
+    FEM_CUDA(cudaFuncSetAttribute(k_gather64, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int64_t rows_per_cta = int64_t(kG64Warps) * kG64Rows;
+    const int64_t blocks = (row_end - row_begin + rows_per_cta - 1) / rows_per_cta;
+    k_gather64<<<unsigned(blocks), kG64Warps * 32, smem, st>>>(gp);
+    FEM_LAUNCH_CHECK("k_gather64");
+    return FEM_OK;
+}
+
+}  // namespace
+}  // namespace fem
+
+extern "C" int fem_assemble_elements(const fem_mesh* mesh, const fem_material* mat, int algo, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
+    if (rc) return rc;
+    FEM_REQUIRE(algo == FEM_ALGO_DD || algo == FEM_ALGO_FP64, "bad algo");
+    if (mesh->n_elem == 0) return FEM_OK;
+    FEM_REQUIRE(algo != FEM_ALGO_DD || (mesh->ne_inv && mesh->slot_map),
+                "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
+    if (algo == FEM_ALGO_DD) return launch_hex8_element_dd(mesh, mat, workspace, as_stream(stream), 0, mesh->n_elem);
+    return launch_hex8_element(mesh, mat, workspace, as_stream(stream), 0, mesh->n_elem);
 }
 
 extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const void* workspace,
@@ -451,25 +784,7 @@ extern "C" int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out*
         FEM_REQUIRE(mesh->n_elem == 0 || mesh->slot_map, "FEM_ALGO_DD needs mesh->slot_map (fem_gather_map)");
         return launch_gather_dd(mesh, out, workspace, as_stream(stream), 0, mesh->n_node);
     }
-    GatherParams gp;
-    gp.n_node = mesh->n_node;
-    gp.indptr = mesh->indptr;
-    gp.indices = mesh->indices;
-    gp.ne_ptr = mesh->ne_ptr;
-    gp.ne_list = mesh->ne_list;
-    gp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
-    gp.rec = static_cast<const double*>(workspace);
-    gp.k_layout = out->k_layout;
-    gp.m_layout = out->m_layout;
-    gp.K = out->K;
-    gp.M = out->M;
-    gp.F = out->F;
-    gp.fixed = out->fixed;
-    gp.loads = out->loads;
-    const int64_t blocks = (mesh->n_node * 32 + 255) / 256;
-    k_gather<<<unsigned(blocks), 256, 0, as_stream(stream)>>>(gp);
-    FEM_LAUNCH_CHECK("k_gather");
-    return FEM_OK;
+    return launch_gather64(mesh, out, workspace, as_stream(stream), 0, mesh->n_node);
 }
 
 extern "C" int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
@@ -508,9 +823,11 @@ extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, 
     if (mesh->n_node == 0) return FEM_OK;
     FEM_REQUIRE(out->algo != FEM_ALGO_DD || mesh->n_elem == 0 || (mesh->ne_inv && mesh->slot_map),
                 "FEM_ALGO_DD needs mesh->ne_inv and mesh->slot_map (fem_gather_map)");
+    FEM_REQUIRE(out->algo == FEM_ALGO_DD || mesh->n_elem == 0 || mesh->slot_map || n_parts == 1,
+                "a split FP64 assembly needs mesh->slot_map (fem_gather_map)");
     cudaStream_t st = as_stream(stream);
     const bool dd = out->algo == FEM_ALGO_DD;
-    const int parts = dd ? n_parts : 1;  // the FP64 kernels run as one part
+    const int parts = n_parts;
     std::vector<cudaEvent_t> done(parts, nullptr);
     cudaStream_t cs = nullptr;
     cudaEvent_t fin = nullptr;
@@ -532,7 +849,8 @@ extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, 
             rc = launch_hex8_element_dd(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
             if (!rc) rc = launch_gather_dd(mesh, out, workspace, st, row_split[q], row_split[q + 1]);
         } else {
-            rc = fem_assemble(mesh, mat, out, workspace, workspace_bytes, stream);
+            rc = launch_hex8_element(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
+            if (!rc) rc = launch_gather64(mesh, out, workspace, st, row_split[q], row_split[q + 1]);
         }
         if (rc) {
             cleanup();
@@ -544,8 +862,8 @@ extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, 
     }
     const int64_t kq = 9, mq = out->m_layout == FEM_LAYOUT_BSR ? 1 : 3;
     for (int q = 0; q < parts; ++q) {
-        const int64_t r0 = dd ? row_split[q] : 0, r1 = dd ? row_split[q + 1] : mesh->n_node;
-        const int64_t b0 = dd ? block_split[q] : 0, b1 = dd ? block_split[q + 1] : mesh->nnzb;
+        const int64_t r0 = row_split[q], r1 = row_split[q + 1];
+        const int64_t b0 = block_split[q], b1 = block_split[q + 1];
         if ((e = cudaStreamWaitEvent(cs, done[q], 0)) != cudaSuccess) return fail(e, "cudaStreamWaitEvent");
         if (K_host && b1 > b0 &&
             (e = cudaMemcpyAsync(K_host + kq * b0, out->K + kq * b0, sizeof(double) * kq * (b1 - b0),

@@ -388,6 +388,82 @@ __global__ void __launch_bounds__(kThreads) k_residual(int64_t nv, const double*
     }
 }
 
+// True residual r = F - A u per scalar row with its rounding scale |F| + |A||u|; per RHS
+// ||r||^2 -> st->norm2 and || |F| + |A||u| ||^2 -> st->anorm2.  kExtra: each row sum is the
+// compensated dot product "Dot2" of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26 (2005)
+// 1955-1988): every product is split exactly into its rounded value and error by an FMA,
+// every addition by Knuth's two-sum, and the errors are summed alongside, so r is as
+// accurate as if formed in twice the FP64 precision and then rounded.  Without kExtra the
+// row sums are plain FP64 FMAs (rounding error up to ~(row length) x 2^-53 x the scale).
+template <int R, bool kExtra>
+__global__ void __launch_bounds__(kThreads) k_residual_ex(const BsrView<double> A, const double* __restrict__ F,
+                                                          const double* __restrict__ u, double* r, double* part,
+                                                          PcgState* st) {
+    const int64_t nv = 3 * A.n * R;
+    double v[2] = {0.0, 0.0};
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ((nv + 31) / 32) * 32;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        if (e < nv) {
+            const int64_t rowc = e / R;  // scalar row 3 node + c
+            const int k = int(e % R);
+            const int64_t node = rowc / 3;
+            const int c = int(rowc - 3 * node);
+            const int64_t rs = __ldg(A.indptr + node);
+            const int L = __ldg(A.indptr + node + 1) - int(rs);
+            const double f = F[e];
+            double s = f, comp = 0.0, sc = fabs(f);
+            for (int l = 0; l < L; ++l) {
+                const int64_t col = __ldg(A.indices + rs + l);
+                const double* ub = u + 3 * col * R + k;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const double m = __ldg(block_value(A, rs, L, l, 3 * c + q));
+                    const double x = ub[q * R];
+                    sc = fma(fabs(m), fabs(x), sc);
+                    if (kExtra) {
+                        const double pr = __dmul_rn(m, x);
+                        const double pe = fma(m, x, -pr);  // m x = pr + pe exactly
+                        const double t = __dsub_rn(s, pr);
+                        const double bb = __dsub_rn(t, s);
+                        const double err = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bb)), __dsub_rn(-pr, bb));
+                        s = t;
+                        comp = __dsub_rn(__dadd_rn(comp, err), pe);
+                    } else {
+                        s = fma(-m, x, s);
+                    }
+                }
+            }
+            const double rv = kExtra ? __dadd_rn(s, comp) : s;
+            r[e] = rv;
+            v[0] = fma(rv, rv, v[0]);
+            v[1] = fma(sc, sc, v[1]);
+        }
+    }
+    if (block_partials<R, 2>(v, part, &st->ticket)) {
+        __shared__ double tot[2][kMaxR];
+        last_block_totals<R, 2>(part, gridDim.x, tot);
+        if (threadIdx.x < R) {
+            st->norm2[threadIdx.x] = tot[0][threadIdx.x];
+            st->anorm2[threadIdx.x] = tot[1][threadIdx.x];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) st->ticket = 0;
+    }
+}
+
+// r_k = 0 for the right-hand sides whose scale s_k is 0 (already converged)
+template <int R>
+__global__ void k_mask_rhs(int64_t nv, const double* __restrict__ s, double* r) {
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nv; e += int64_t(gridDim.x) * blockDim.x)
+        if (!(s[e % R] > 0.0)) r[e] = 0.0;
+}
+
+// u += d
+__global__ void k_add(int64_t n, const double* __restrict__ d, double* u) {
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < n; e += int64_t(gridDim.x) * blockDim.x)
+        u[e] += d[e];
+}
+
 // b32 = r / s_k (s_k = 0 -> zero right-hand side)
 template <int R>
 __global__ void k_scale_cast(int64_t nv, const double* __restrict__ r, const double* __restrict__ s, float* b32) {
@@ -411,7 +487,7 @@ __global__ void k_zero(int64_t n, double* u) {
 
 // ---- host side ------------------------------------------------------------------------------
 struct Layout {
-    size_t state, part, v64[5], v32[6], m32, scale, total;
+    size_t state, part, v64[6], v32[6], m32, scale, total;
 };
 
 size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
@@ -427,7 +503,7 @@ Layout layout(int64_t n, int R, int mixed) {
     const size_t nv = size_t(3) * n * R;
     L.state = take(sizeof(PcgState));
     L.part = take(sizeof(double) * kMaxCtas * kSlots * kMaxR);
-    for (int i = 0; i < 5; ++i) L.v64[i] = take(mixed ? (i < 2 ? sizeof(double) * nv : 0) : sizeof(double) * nv);
+    for (int i = 0; i < 6; ++i) L.v64[i] = take(mixed ? (i < 2 ? sizeof(double) * nv : 0) : sizeof(double) * nv);
     for (int i = 0; i < 6; ++i) L.v32[i] = take(mixed ? sizeof(float) * nv : 0);
     L.m32 = take(mixed ? sizeof(float) * 9 * n : 0);
     L.scale = take(sizeof(double) * kMaxR);
@@ -491,9 +567,12 @@ struct InnerResult {
 
 // Initialises the solver state (init(s)), then runs `unroll` iterations at a time
 // (iters(count, s), replayed as one CUDA graph when use_graph) until the state says done.
+// stall > 0: the solve also ends, with FEM_ERR_NOT_CONVERGED, once the largest relative
+// recursive residual over the active right-hand sides has not halved within `stall`
+// iterations (checked at every host check, i.e. every `unroll` iterations).
 template <typename Init, typename Iters>
 int pcg_drive(const Init& init, const Iters& iters, PcgState* st, int maxit, int use_graph, int unroll,
-              cudaStream_t s, InnerResult* res) {
+              cudaStream_t s, InnerResult* res, int stall = 0) {
     int rc0 = init(s);
     if (rc0) return rc0;
     unroll = std::max(1, std::min(unroll, 256));
@@ -511,6 +590,9 @@ int pcg_drive(const Init& init, const Iters& iters, PcgState* st, int maxit, int
     }
     PcgState h;
     int launched = 0, rc = FEM_OK;
+    bool stalled = false;
+    double ref = -1.0;  // residual at the last halving
+    int ref_it = 0;
     // the device caps iterations at maxit; the host loop is bounded by the same count
     while (launched < maxit + unroll) {
         if (exec) {
@@ -524,18 +606,31 @@ int pcg_drive(const Init& init, const Iters& iters, PcgState* st, int maxit, int
         if (rc) break;
         rc = cuda_status(cudaStreamSynchronize(s), "state sync");
         if (rc || h.done) break;
+        if (stall > 0) {
+            double w = 0.0;
+            for (int k = 0; k < kMaxR; ++k)
+                if (h.active[k] && h.bb[k] > 0.0) w = std::max(w, sqrt(h.rr[k] / h.bb[k]));
+            if (ref < 0.0 || w <= 0.5 * ref) {
+                ref = w;
+                ref_it = h.it;
+            } else if (h.it - ref_it >= stall) {
+                stalled = true;
+                break;
+            }
+        }
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (rc) return rc;
     res->iters = h.it;
-    res->status = h.done ? h.status : FEM_ERR_MAXITER;
+    res->status = h.done ? h.status : (stalled ? FEM_ERR_NOT_CONVERGED : FEM_ERR_MAXITER);
     return FEM_OK;
 }
 
 // Runs PCG on (A, M) with right-hand side b into x; vectors r z p q are workspace.
 template <typename T, int R>
 int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
-             double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res) {
+             double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res,
+             int stall = 0) {
     auto init = [&](cudaStream_t ss) -> int {
         k_init<T, R><<<vec_grid(A.n * R), kThreads, 0, ss>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
         FEM_LAUNCH_CHECK("k_init");
@@ -544,7 +639,7 @@ int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p
     auto iters = [&](int count, cudaStream_t ss) -> int {
         return launch_iterations<T, R>(A, M, x, r, z, p, q, part, st, variant, count, ss);
     };
-    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res);
+    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res, stall);
 }
 
 // The same with the multigrid V-cycle as the preconditioner.  T = float: the FP32 inner
@@ -553,7 +648,7 @@ int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p
 template <typename T, int R>
 int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, const T* b, T* x, T* r, T* z, T* p,
                  T* q, double* part, PcgState* st, double rtol, int maxit, int variant, int use_graph, int unroll,
-                 cudaStream_t s, InnerResult* res) {
+                 cudaStream_t s, InnerResult* res, int stall = 0) {
     const int64_t nv = 3 * A.n * R;
     const unsigned gv = vec_grid(nv);
     constexpr bool f64 = sizeof(T) == 8;
@@ -583,7 +678,7 @@ int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, c
         FEM_LAUNCH_CHECK("pcg iteration (amg)");
         return FEM_OK;
     };
-    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res);
+    return pcg_drive(init, iters, st, maxit, use_graph, unroll, s, res, stall);
 }
 
 template <int R>
@@ -594,16 +689,20 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
     const Layout L = layout(n, R, o->mixed);
     PcgState* st = reinterpret_cast<PcgState*>(ws + L.state);
     double* part = reinterpret_cast<double*>(ws + L.part);
+    double* scale = reinterpret_cast<double*>(ws + L.scale);
     BsrView<double> K64{n, A64->indptr, A64->indices, static_cast<const double*>(A64->vals),
                         rsoa_kind(A64->layout)};
     const int maxit = std::max(1, o->maxit);
+    const bool extra = o->residual == FEM_RESIDUAL_EXTRA;
     InnerResult ir{0, FEM_OK};
     PcgState h;
-    auto true_residual = [&](const double* u, double* y, double* r) -> int {
-        int rc = bsr_spmv_any(A64, R, u, y, o->spmv_variant, s);
-        if (rc) return rc;
-        k_residual<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, F, y, r, part, st);
-        FEM_LAUNCH_CHECK("k_residual");
+    // r = F - K u (FP64 or compensated), its norms and rounding scales -> h
+    auto true_residual = [&](const double* u, double* r) -> int {
+        if (extra)
+            k_residual_ex<R, true><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
+        else
+            k_residual_ex<R, false><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
+        FEM_LAUNCH_CHECK("k_residual_ex");
         FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
         FEM_CUDA(cudaStreamSynchronize(s));
         return FEM_OK;
@@ -612,42 +711,92 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
     FEM_CUDA(cudaMemsetAsync(st, 0, sizeof(PcgState), s));
     double bnorm[kMaxR];
     {
-        // ||F_k||: residual of u = 0
-        double* y = reinterpret_cast<double*>(ws + L.v64[0]);
-        double* r = reinterpret_cast<double*>(ws + L.v64[1]);
-        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, y);
-        k_residual<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, F, y, r, part, st);
-        FEM_LAUNCH_CHECK("k_residual");
+        // ||F_k||: the residual of u = 0
+        double* z0 = reinterpret_cast<double*>(ws + L.v64[0]);
+        double* r0 = reinterpret_cast<double*>(ws + L.v64[1]);
+        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, z0);
+        FEM_LAUNCH_CHECK("k_zero");
+        k_residual_ex<R, false><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, z0, r0, part, st);
+        FEM_LAUNCH_CHECK("k_residual_ex");
         FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
         FEM_CUDA(cudaStreamSynchronize(s));
         for (int k = 0; k < R; ++k) bnorm[k] = sqrt(h.norm2[k]);
     }
+    // relative true residual per RHS from h, worst over the RHS
+    auto rel = [&](int k) { return bnorm[k] > 0 ? sqrt(h.norm2[k]) / bnorm[k] : 0.0; };
+    auto worst_rel = [&]() {
+        double w = 0.0;
+        for (int k = 0; k < R; ++k) w = std::max(w, rel(k));
+        return w;
+    };
+    // scale[k] = ||r_k|| for the RHS still above rtol, 0 for the others; returns how many
+    auto set_active = [&](double* sc) {
+        int any = 0;
+        for (int k = 0; k < R; ++k) {
+            const bool act = bnorm[k] > 0 && rel(k) > o->rtol;
+            sc[k] = act ? sqrt(h.norm2[k]) : 0.0;
+            any += act;
+        }
+        return any;
+    };
     int total_iters = 0, outer = 0, status = FEM_OK;
+    const int max_outer = std::max(1, o->max_outer);
     if (!o->mixed) {
+        // FP64 PCG on K U = F, then residual replacement: while the true residual is above
+        // rtol (the recursive residual drifts from it on ill-conditioned systems), solve
+        // K d = r for the correction and add it (at most max_outer solves in all; stop when
+        // a step does not halve the worst residual).
         double* r = reinterpret_cast<double*>(ws + L.v64[0]);
         double* z = reinterpret_cast<double*>(ws + L.v64[1]);
         double* p = reinterpret_cast<double*>(ws + L.v64[2]);
         double* q = reinterpret_cast<double*>(ws + L.v64[3]);
-        int rc;
-        if (amg) {
-            const BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
-                                     rsoa_kind(A32->layout)};
-            rc = pcg_core_amg<double, R>(K64, K32, amg, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
-                                         o->use_graph, o->unroll, s, &ir);
-        } else {
-            rc = pcg_core<double, R>(K64, M64, F, U, r, z, p, q, part, st, o->rtol, maxit, o->spmv_variant,
-                                     o->use_graph, o->unroll, s, &ir);
-        }
+        double* rt = reinterpret_cast<double*>(ws + L.v64[4]);
+        double* d = reinterpret_cast<double*>(ws + L.v64[5]);
+        auto core = [&](const double* b, double* x, double tol, int cap) -> int {
+            if (amg) {
+                const BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
+                                         rsoa_kind(A32->layout)};
+                return pcg_core_amg<double, R>(K64, K32, amg, b, x, r, z, p, q, part, st, tol, cap, o->spmv_variant,
+                                               o->use_graph, o->unroll, s, &ir, o->stall_window);
+            }
+            return pcg_core<double, R>(K64, M64, b, x, r, z, p, q, part, st, tol, cap, o->spmv_variant,
+                                       o->use_graph, o->unroll, s, &ir, o->stall_window);
+        };
+        int rc = core(F, U, o->rtol, maxit);
         if (rc) return rc;
         total_iters = ir.iters;
-        outer = 1;
         status = ir.status;
-        rc = true_residual(U, q, r);
-        if (rc) return rc;
+        outer = 1;
+        if ((rc = true_residual(U, rt))) return rc;
+        double prev = worst_rel();
+        while (status == FEM_OK && outer < max_outer && total_iters < maxit) {
+            double sc[kMaxR];
+            if (!set_active(sc)) break;
+            // the correction must bring ||r_k|| down to rtol ||F_k|| for every active RHS
+            double tol = 0.5;
+            for (int k = 0; k < R; ++k)
+                if (sc[k] > 0) tol = std::min(tol, o->rtol * bnorm[k] / sc[k]);
+            tol = std::max(tol, 1e-15);
+            FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
+            k_mask_rhs<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, scale, rt);
+            FEM_LAUNCH_CHECK("k_mask_rhs");
+            if ((rc = core(rt, d, tol, maxit - total_iters))) return rc;
+            total_iters += ir.iters;
+            ++outer;
+            if (ir.status == FEM_ERR_BREAKDOWN || ir.status == FEM_ERR_NOT_SPD) {
+                status = ir.status;
+                break;
+            }
+            k_add<<<vec_grid(nv), kThreads, 0, s>>>(nv, d, U);
+            FEM_LAUNCH_CHECK("k_add");
+            if ((rc = true_residual(U, rt))) return rc;
+            const double w = worst_rel();
+            if (!(w < 0.5 * prev)) break;  // no further progress: the FP64 floor is reached
+            prev = w;
+        }
     } else {
         BsrView<float> K32{n, A32->indptr, A32->indices, static_cast<const float*>(A32->vals),
                            rsoa_kind(A32->layout)};
-        double* y = reinterpret_cast<double*>(ws + L.v64[0]);
         double* r64 = reinterpret_cast<double*>(ws + L.v64[1]);
         float* b32 = reinterpret_cast<float*>(ws + L.v32[0]);
         float* d32 = reinterpret_cast<float*>(ws + L.v32[1]);
@@ -656,31 +805,18 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
         float* pp = reinterpret_cast<float*>(ws + L.v32[4]);
         float* qq = reinterpret_cast<float*>(ws + L.v32[5]);
         float* M32 = reinterpret_cast<float*>(ws + L.m32);
-        double* scale = reinterpret_cast<double*>(ws + L.scale);
         int rc = amg ? FEM_OK : fem_convert_f64_to_f32(M64, M32, 9 * n, s);
         if (rc) return rc;
         k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, U);
         FEM_LAUNCH_CHECK("k_zero");
-        rc = true_residual(U, y, r64);
+        rc = true_residual(U, r64);
         if (rc) return rc;
-        const int max_outer = std::max(1, o->max_outer);
         double prev = 1e300;
         for (outer = 0; outer < max_outer; ++outer) {
-            double sc[kMaxR], worst = 0.0;
-            int any = 0;
-            for (int k = 0; k < R; ++k) {
-                const double rn = sqrt(h.norm2[k]);
-                const double rel = bnorm[k] > 0 ? rn / bnorm[k] : 0.0;
-                worst = std::max(worst, rel);
-                const bool act = bnorm[k] > 0 && rel > o->rtol;
-                sc[k] = act ? rn : 0.0;
-                any |= act;
-            }
-            if (!any) break;
-            if (outer > 0 && !(worst < 0.5 * prev)) {
-                status = FEM_ERR_NOT_CONVERGED;  // refinement stalled
-                break;
-            }
+            double sc[kMaxR];
+            if (!set_active(sc)) break;
+            const double worst = worst_rel();
+            if (outer > 0 && !(worst < 0.5 * prev)) break;  // refinement stalled
             prev = worst;
             FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
             k_scale_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, r64, scale, b32);
@@ -688,20 +824,24 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
             if (amg)
                 rc = pcg_core_amg<float, R>(K32, K32, amg, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
                                             std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll,
-                                            s, &ir);
+                                            s, &ir, o->stall_window);
             else
                 rc = pcg_core<float, R>(K32, M32, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
                                         std::max(1, o->inner_maxit), o->spmv_variant32, o->use_graph, o->unroll, s,
-                                        &ir);
+                                        &ir, o->stall_window);
             if (rc) return rc;
             total_iters += ir.iters;
+            if (o->stall_window > 0 && ir.status == FEM_ERR_NOT_CONVERGED) {
+                status = FEM_ERR_NOT_CONVERGED;  // the inner solve stalled
+                break;
+            }
             if (ir.status == FEM_ERR_BREAKDOWN || ir.status == FEM_ERR_NOT_SPD) {
                 status = ir.status;
                 break;
             }
             k_axpy_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, scale, d32, U);
             FEM_LAUNCH_CHECK("k_axpy_cast");
-            rc = true_residual(U, y, r64);
+            rc = true_residual(U, r64);
             if (rc) return rc;
             if (total_iters >= maxit) {
                 status = FEM_ERR_MAXITER;
@@ -709,16 +849,19 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
             }
         }
     }
-    double worst = 0.0;
-    for (int k = 0; k < R; ++k) {
-        const double rel = bnorm[k] > 0 ? sqrt(h.norm2[k]) / bnorm[k] : 0.0;
-        worst = std::max(worst, rel);
-    }
-    if (status == FEM_OK && o->mixed && worst > o->rtol) status = FEM_ERR_MAXITER;
+    // The status is judged on the true residual of the returned U, whatever the mode: a solve
+    // that stopped above rtol (iteration cap, stall, recursive residual drifting from the true
+    // one) does not report success.
+    const double worst = worst_rel();
+    double floor_rel = 0.0;
+    for (int k = 0; k < R; ++k)
+        if (bnorm[k] > 0) floor_rel = std::max(floor_rel, 0x1p-53 * sqrt(h.anorm2[k]) / bnorm[k]);
+    if (status == FEM_OK && worst > o->rtol) status = total_iters >= maxit ? FEM_ERR_MAXITER : FEM_ERR_NOT_CONVERGED;
     out->status = status;
     out->iterations = total_iters;
     out->outer = outer;
     out->relres = worst;
+    out->floor = floor_rel;
     return FEM_OK;
 }
 

@@ -15,6 +15,7 @@ constexpr int kSlots = 3;
 struct PcgState {
     double rz[kMaxR], pq[kMaxR], alpha[kMaxR], beta[kMaxR], bb[kMaxR], rr[kMaxR], tol2[kMaxR];
     double norm2[kMaxR];
+    double anorm2[kMaxR];  // || |F| + |A||u| ||^2 of the last true residual (its rounding scale)
     int active[kMaxR];
     int iters[kMaxR];
     int it, done, status, maxit;

@@ -29,6 +29,49 @@ from .model import _dptr
 from .solve import DeviceSystem, padded_nrhs
 
 
+class _PhaseTimes:
+    """Accumulates device time per phase with CUDA events on the launch stream (read once at
+    the end of the solve) and host time for host-side phases."""
+
+    def __init__(self, device):
+        self.device = device
+        self.pairs = {}
+        self.host = {}
+
+    def device_phase(self, name):
+        t = self
+
+        class _Ctx:
+            def __enter__(self_):
+                s = torch.cuda.current_stream(t.device)
+                self_.e0 = torch.cuda.Event(enable_timing=True)
+                self_.e1 = torch.cuda.Event(enable_timing=True)
+                self_.e0.record(s)
+
+            def __exit__(self_, *a):
+                self_.e1.record(torch.cuda.current_stream(t.device))
+                t.pairs.setdefault(name, []).append((self_.e0, self_.e1))
+        return _Ctx()
+
+    def host_phase(self, name):
+        import time
+        t = self
+
+        class _Ctx:
+            def __enter__(self_):
+                self_.t0 = time.perf_counter()
+
+            def __exit__(self_, *a):
+                t.host[name] = t.host.get(name, 0.0) + time.perf_counter() - self_.t0
+        return _Ctx()
+
+    def result_ms(self):
+        torch.cuda.synchronize(self.device)
+        out = {k: sum(a.elapsed_time(b) for a, b in v) for k, v in self.pairs.items()}
+        out.update({k: 1e3 * v for k, v in self.host.items()})
+        return out
+
+
 class Eigen_solver:
     """Drop-in for SOLVE_eigen.Eigen_solver (Qtype 0)."""
 
@@ -94,34 +137,55 @@ class Eigen_solver:
         u = torch.as_tensor(np.asarray(u0, dtype=np.float64), device=dev).reshape(n, b)
         Q = torch.zeros((n, m), dtype=torch.float64, device=dev)
         T = np.zeros((m, m))
-        v = torch.linalg.cholesky(u.T @ self._apply_M(u)).T         # upper, u^T M u = v^T v
-        u = torch.linalg.solve_triangular(v, u, upper=True, left=False)
+        ph = _PhaseTimes(dev)
+        with ph.device_phase("m_products"):
+            Mu = self._apply_M(u)
+        with ph.device_phase("cholesky"):
+            v = torch.linalg.cholesky(u.T @ Mu).T                       # upper, u^T M u = v^T v
+            u = torch.linalg.solve_triangular(v, u, upper=True, left=False)
         Q[:, :b] = u
         iters = 0
         for i in range(steps):
-            w, st = S.solve(F=self._apply_M(u), rtol=rtol, mixed=mixed, precond=pc)
+            with ph.device_phase("m_products"):
+                Mu = self._apply_M(u)
+            with ph.device_phase("k_solves"):
+                w, st = S.solve(F=Mu, rtol=rtol, mixed=mixed, precond=pc)
             if st["status"] != 0:
                 raise _lib.FemError(st["status"], f"K solve of Lanczos step {i}: {st['status_text']}")
             iters += st["iterations"]
             w = w.reshape(n, b)
-            Tii = u.T @ self._apply_M(w)
-            T[i * b:(i + 1) * b, i * b:(i + 1) * b] = Tii.cpu().numpy()
-            w = w - u @ Tii
+            with ph.device_phase("m_products"):
+                Mw = self._apply_M(w)
+            with ph.device_phase("reorth_gemms"):
+                Tii = u.T @ Mw
+                w = w - u @ Tii
+            with ph.host_phase("host_copies_eigh"):
+                T[i * b:(i + 1) * b, i * b:(i + 1) * b] = Tii.cpu().numpy()
             if i >= steps - 1:
                 break
             Qi = Q[:, :(i + 1) * b]
             for _ in range(2):
-                w = w - Qi @ (Qi.T @ self._apply_M(w))
-            t = torch.linalg.cholesky(w.T @ self._apply_M(w)).T
-            T[(i + 1) * b:(i + 2) * b, i * b:(i + 1) * b] = t.cpu().numpy()
-            T[i * b:(i + 1) * b, (i + 1) * b:(i + 2) * b] = t.T.cpu().numpy()
-            u = torch.linalg.solve_triangular(t, w, upper=True, left=False)
+                with ph.device_phase("m_products"):
+                    Mw = self._apply_M(w)
+                with ph.device_phase("reorth_gemms"):
+                    w = w - Qi @ (Qi.T @ Mw)
+            with ph.device_phase("m_products"):
+                Mw = self._apply_M(w)
+            with ph.device_phase("cholesky"):
+                t = torch.linalg.cholesky(w.T @ Mw).T
+                u = torch.linalg.solve_triangular(t, w, upper=True, left=False)
+            with ph.host_phase("host_copies_eigh"):
+                tn = t.cpu().numpy()
+            T[(i + 1) * b:(i + 2) * b, i * b:(i + 1) * b] = tn
+            T[i * b:(i + 1) * b, (i + 1) * b:(i + 2) * b] = tn.T
             Q[:, (i + 1) * b:(i + 2) * b] = u
-        ev, vec = np.linalg.eigh(T)
+        with ph.host_phase("host_copies_eigh"):
+            ev, vec = np.linalg.eigh(T)
         lam = 1.0 / ev
         order = np.argsort(lam)[:num_eigen]
-        X = Q @ torch.as_tensor(vec[:, order], device=dev)
-        self.last_stats = {"steps": steps, "solve_iterations": iters}
+        with ph.device_phase("reorth_gemms"):
+            X = Q @ torch.as_tensor(vec[:, order], device=dev)
+        self.last_stats = {"steps": steps, "solve_iterations": iters, "phase_ms": ph.result_ms()}
         return torch.as_tensor(lam[order], device=dev), X
 
     def Solve_cpu(self, num_eigen=100, num_block=10):

@@ -197,6 +197,14 @@ class DeviceSystem:
             self._amg = AmgHierarchy(self.lib, self.n, P.SmNode, P.ReNode, K, xyz, self.stream, **opts)
         return self._amg
 
+    def amg_variant(self, **opts) -> AmgHierarchy:
+        """A separate multigrid hierarchy of K built with ``opts`` (not cached; pass it to
+        ``solve(precond=...)`` and close it when done)."""
+        xyz = self.model.mesh.xyz.cpu().numpy()
+        K = self.K64.reshape(-1).cpu().numpy()
+        P = self.model.Physics
+        return AmgHierarchy(self.lib, self.n, P.SmNode, P.ReNode, K, xyz, self.stream, **opts)
+
     def spmv(self, x: torch.Tensor, fp32=False, nrhs=1) -> torch.Tensor:
         A = self._A32 if fp32 else self.A64
         if fp32:
@@ -230,12 +238,20 @@ class DeviceSystem:
         return self._variant[key]
 
     def solve(self, F=None, rtol=1e-10, maxit=50000, mixed=True, precond=None, use_graph=True, unroll=16,
-              inner_rtol=1e-4, inner_maxit=20000, max_outer=40):
+              inner_rtol=1e-4, inner_maxit=20000, max_outer=40, residual="fp64", stall_window=0):
         """Solve K U = F.  F: device/host array (3N,) or (3N, R) (default: the assembled F).
 
-        precond: (N, 9) FP64 blocks (default block Jacobi), or "amg" (multigrid V-cycle; with
+        precond: (N, 9) FP64 blocks (default block Jacobi), "amg" (multigrid V-cycle; with
         mixed=True inside the FP32 inner solve, falling back to the FP64 flexible-CG form when
-        the refinement stalls).  Returns (U (3N,) or (3N, R) device tensor, stats dict)."""
+        the refinement stalls) or an AmgHierarchy of this matrix (amg_variant).  residual: "fp64" or "extra" -- how the true residual F - K U
+        that decides convergence and drives the refinement is formed ("extra": compensated,
+        as accurate as twice-FP64 arithmetic).  Returns (U (3N,) or (3N, R) device tensor,
+        stats dict).  stall_window > 0 ends a solve whose worst relative residual has not
+        halved in that many iterations (status FEM_ERR_NOT_CONVERGED).  stats["status"] is 0 only when ||F - K U|| / ||F|| <= rtol for every
+        right-hand side, and stats["floor"] is the residual that rounding U to FP64 alone
+        leaves (2^-53 || |F| + |K||U| || / ||F||, max over RHS)."""
+        if residual not in ("fp64", "extra"):
+            raise ValueError("residual must be 'fp64' or 'extra'")
         if F is None:
             F = self.F
         F = torch.as_tensor(F, dtype=torch.float64, device=self.device)
@@ -247,9 +263,9 @@ class DeviceSystem:
             F2 = torch.cat([F2, torch.zeros((3 * self.n, Rp - R), dtype=torch.float64, device=self.device)], 1)
         F2 = F2.contiguous()
         U = torch.empty_like(F2)
-        use_amg = isinstance(precond, str) and precond == "amg"
+        use_amg = isinstance(precond, AmgHierarchy) or (isinstance(precond, str) and precond == "amg")
         if use_amg:
-            amg = self.amg()
+            amg = precond if isinstance(precond, AmgHierarchy) else self.amg()
             self.K32()
             P = None
         else:
@@ -263,7 +279,8 @@ class DeviceSystem:
             self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         opts = FemPcgOpts(Rp, int(mixed), float(rtol), int(maxit), float(inner_rtol), int(inner_maxit),
                           int(max_outer), int(use_graph), int(unroll), self.variant(False, Rp),
-                          self.variant(True, Rp) if mixed else 0)
+                          self.variant(True, Rp) if mixed else 0,
+                          _lib.RESIDUAL_EXTRA if residual == "extra" else _lib.RESIDUAL_FP64, int(stall_window))
         st = FemPcgStats()
         A32 = ctypes.byref(self._A32) if (mixed or use_amg) else None
         if use_amg:
@@ -276,11 +293,12 @@ class DeviceSystem:
                                               self._ws.numel(), self.stream), "fem_pcg_solve")
         stats = {"status": st.status, "status_text": _STATUS.get(st.status, str(st.status)),
                  "iterations": st.iterations, "outer": st.outer, "relres": st.relres, "time_ms": st.time_ms,
-                 "nrhs": R, "mixed": bool(mixed), "precond": "amg" if use_amg else "block"}
+                 "floor": st.floor, "nrhs": R, "mixed": bool(mixed), "precond": "amg" if use_amg else "block",
+                 "residual": residual, "stall_window": int(stall_window)}
         if use_amg and mixed and st.status == _lib.FEM_ERR_NOT_CONVERGED:
             # FP32 refinement stalled (condition number beyond FP32): FP64 flexible CG instead
-            U2, st2 = self.solve(F=F if squeeze else F2[:, :R], rtol=rtol, maxit=maxit, mixed=False, precond="amg",
-                                 use_graph=use_graph, unroll=unroll)
+            U2, st2 = self.solve(F=F if squeeze else F2[:, :R], rtol=rtol, maxit=maxit, mixed=False, precond=precond,
+                                 use_graph=use_graph, unroll=unroll, max_outer=max_outer, residual=residual)
             st2["fallback_from"] = stats
             return U2, st2
         U = U[:, :R]
@@ -339,10 +357,13 @@ class Static_solver:
                            "converged": res[-1] <= max_errs}
         return U.cpu().numpy()
 
-    def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, **kw):
+    def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, stall_window=256, **kw):
         """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'amg' (multigrid
-        V-cycle), 'learned' (uses ``self.Model.learned_precond`` (N, 9) if set, falling back to
-        block Jacobi when the learned solve does not converge) or an (N, 9) array."""
+        V-cycle), 'learned' (uses ``self.Model.learned_precond`` (N, 9) if set) or an (N, 9)
+        array.  The learned solve runs with a stall detector: when its worst relative residual
+        has not halved within ``stall_window`` iterations (or it fails otherwise) the solve
+        switches to plain block Jacobi from the start; ``last_stats["fallback_from"]`` then
+        holds the abandoned attempt."""
         if self.Qtype != 0:
             raise ValueError("Solve_gpu is the linear solve; Qtype=1 uses Solve_cpu / Solve_nonlinear")
         S = self._system()
@@ -360,7 +381,8 @@ class Static_solver:
                 raise ValueError("precond must be 'bj', 'amg', 'learned' or an (N, 9) array")
         else:
             P = precond
-        U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P, **kw)
+        U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P,
+                        stall_window=stall_window if fallback else 0, **kw)
         if fallback and st["status"] != 0:
             U, st2 = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=None, **kw)
             st2["fallback_from"] = st
@@ -373,14 +395,23 @@ class Static_solver:
         to a relative residual of 1e-12 (the reference used a direct factorisation, which
         always returns a solution): mixed block-Jacobi PCG first (capped at 20,000
         iterations), and when that does not converge (slender or stretched meshes) the FP64
-        multigrid solve to 1e-10, whose residual is near the FP64 floor of such systems;
-        ``last_stats["fallback_from"]`` then holds the first attempt.  Qtype 1 runs the
-        large-displacement Newton iteration (Solve_nonlinear)."""
+        multigrid solve with compensated residuals to 1e-12 or as far as FP64 allows;
+        ``last_stats["fallback_from"]`` then holds the first attempt.  When the fallback also
+        stops above 1e-12, a RuntimeWarning gives its residual and the FP64 floor
+        (``last_stats["floor"]``): the displacement is then as accurate as FP64 storage permits
+        when the two are close.  Qtype 1 runs the large-displacement Newton iteration
+        (Solve_nonlinear)."""
         if self.Qtype == 1:
             return self.Solve_nonlinear(max_errs=max_errs, max_iters=max_iters)
         U = self.Solve_gpu(rtol=1e-12, mixed=True, maxit=20000)
         if self.last_stats["status"] != 0:
             first = self.last_stats
-            U = self.Solve_gpu(rtol=1e-10, mixed=False, precond="amg")
+            U = self.Solve_gpu(rtol=1e-12, mixed=False, precond="amg", residual="extra", max_outer=8)
             self.last_stats["fallback_from"] = first
+            st = self.last_stats
+            if st["status"] != 0:
+                import warnings
+                warnings.warn(f"static solve stopped at relative residual {st['relres']:.3e} > 1e-12 "
+                              f"({st['status_text']}); FP64 floor of this system {st['floor']:.3e}",
+                              RuntimeWarning, stacklevel=2)
         return U

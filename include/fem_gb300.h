@@ -203,7 +203,10 @@ int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, const double* u
  * scratch is a 24 MiB array built into the library, reserved on each GPU that loads it until
  * the process exits, so meshes are limited to FEM_STRESS_NOALLOC_MAX_ELEMS elements (larger
  * ones return FEM_ERR_WORKSPACE).  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  All calls share the one array:
+ * address and keeps it for the life of the process; make that first call before any stream
+ * capture.  The kept address belongs to the device's context at that time: after
+ * cudaDeviceReset (a new primary context) it is stale, so a program that resets a device does
+ * not call this entry point on it again without reloading the library.  All calls share the one array:
  * calls that can overlap on the GPU (other streams, other host threads) race and must be
  * serialised by the caller.  Nothing in the array needs clearing between calls.  It calls no
  * allocator. */
@@ -264,21 +267,37 @@ typedef struct fem_pcg_opts {
     int unroll;         /* iterations per graph / per host convergence check                 */
     int spmv_variant;   /* launch variant of the FP64 SpMV (fem_spmv_autotune)               */
     int spmv_variant32; /* launch variant of the FP32 SpMV                                   */
+    int residual;       /* true residual F - K U: FEM_RESIDUAL_FP64 (0) or FEM_RESIDUAL_EXTRA */
+    int stall_window;   /* > 0: stop with FEM_ERR_NOT_CONVERGED when the worst relative
+                           (recursive) residual has not halved in this many iterations    */
 } fem_pcg_opts;
+
+/* How the solver forms the true residual r = F - K U that decides convergence and drives
+ * the refinement / residual-replacement steps.  FEM_RESIDUAL_EXTRA evaluates each row as a
+ * compensated dot product (as accurate as twice-FP64 arithmetic), so the refinement can drive
+ * the forward error of U to the FP64 rounding level even where ||F - K U|| / ||F|| itself
+ * cannot fall below the floor reported in fem_pcg_stats.floor. */
+#define FEM_RESIDUAL_FP64 0
+#define FEM_RESIDUAL_EXTRA 1
 
 typedef struct fem_pcg_stats {
     int status;        /* FEM_OK, FEM_ERR_MAXITER, FEM_ERR_NOT_CONVERGED, FEM_ERR_NOT_SPD, ... */
     int iterations;    /* PCG iterations executed (sum of inner iterations when mixed)        */
     int outer;         /* refinement steps (1 for FP64 PCG)                                   */
-    double relres;     /* max over RHS of the FP64 true residual ||F - K U|| / ||F||          */
+    double relres;     /* max over RHS of the true residual ||F - K U|| / ||F||               */
     double time_ms;    /* device time of the solve (CUDA events)                              */
+    double floor;      /* max over RHS of 2^-53 || |F| + |K||U| || / ||F||: the residual that
+                          rounding U to FP64 alone leaves; an rtol below it cannot be met    */
 } fem_pcg_stats;
 
 /* Solve K U = F (SOLVE_static.py:31-33; Pardiso replaced by PCG).  precond: [n_brow][9]
  * FP64 preconditioner blocks applied as z_i = P_i r_i (block Jacobi from fem_block_jacobi,
  * or a learned SPD correction).  F, U: [n_brow][3][nrhs] FP64.  A32 (FP32 copy of A64) is
  * required when opts->mixed.  The call returns FEM_OK when it ran; stats->status tells
- * whether the tolerance was met. */
+ * whether the tolerance was met: FEM_OK only when the true residual of the returned U
+ * (formed as opts->residual says) is at most rtol for every right-hand side.  FP64 mode
+ * (mixed = 0) runs PCG, then residual-replacement steps (K d = F - K U, U += d) while the
+ * true residual is above rtol, at most max_outer solves in all. */
 size_t fem_pcg_workspace_bytes(int64_t n_brow, int nrhs, int mixed);
 int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond, const double* F, double* U,
                   const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,

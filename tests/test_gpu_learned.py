@@ -8,6 +8,7 @@ import scipy.sparse.linalg as spla
 import torch
 
 import fem_taichi_gb300 as F
+from fem_taichi_gb300 import _lib
 from fem_taichi_gb300.learned import LearnedPreconditioner, NodeData
 from oracle import mlp_oracle as MO
 from tests.fixtures import STEEL
@@ -101,3 +102,27 @@ def test_train_reduces_loss_and_learned_solve_is_exact():
     K = M.Get_MatrixKL()
     Ur = spla.spsolve(K.tocsc(), M.Get_VectorF())
     assert np.linalg.norm(U - Ur) / np.linalg.norm(Ur) <= 1e-8, sol.last_stats
+
+
+def test_stalled_learned_solve_switches_to_block_jacobi():
+    """Solve_gpu(precond='learned') watches the learned solve: an SPD preconditioner whose
+    blocks are block Jacobi scaled by factors spanning 16 decades stagnates; the solve is
+    abandoned once its residual stops halving (long before the iteration cap) and plain
+    block Jacobi takes over, reaching the direct solution."""
+    P = F.hex_block(12, 10, 5, size=(12.0, 10.0, 5.0), jitter=0.1, seed=5, fix="zmin", load_face="zmax",
+                    load=(0, 0, -1))
+    M = F.Model("stall", P, STEEL)
+    S = F.DeviceSystem(M)
+    scale = 10.0 ** np.random.default_rng(1).uniform(-8, 8, size=P.Num_Node)
+    M.learned_precond = S.block_jacobi() * torch.from_numpy(scale).to(S.device)[:, None]
+    sol = F.Static_solver(M)
+    U = sol.Solve_gpu(rtol=1e-12, precond="learned", mixed=False, maxit=20000, stall_window=64)
+    st = sol.last_stats
+    first = st.get("fallback_from")
+    assert first is not None and first["status"] == _lib.FEM_ERR_NOT_CONVERGED, st
+    assert first["iterations"] < 2000, first
+    assert st["status"] == 0 and st["precond"] == "block", st
+    K = M.Get_MatrixKL()
+    Ur = spla.spsolve(K.tocsc(), M.Get_VectorF())
+    assert np.linalg.norm(U - Ur) / np.linalg.norm(Ur) <= 1e-8, st
+    print("stall detected after", first["iterations"], "iterations; block Jacobi:", st["iterations"])
