@@ -59,11 +59,12 @@ def concat(datasets):
     return b
 
 
-def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda"):
+def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda", min_nodes=20_000,
+             max_nodes=200_000):
     t0 = time.perf_counter()
     data = []
     nodes = 0
-    for P, mat in training_meshes(count, seed):
+    for P, mat in training_meshes(count, seed, min_nodes=min_nodes, max_nodes=max_nodes):
         S = DeviceSystem(Model(P.name, P, mat, device=device))
         data.append(NodeData(S, n_probes=n_probes, seed=len(data)))
         nodes += P.Num_Node

@@ -161,6 +161,9 @@ SIGNATURES = {
                                 c_void_p]),
     "fem_mlp_loss_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p, c_void_p,
                                   ctypes.POINTER(c_int), c_void_p]),
+    "fem_mlp_backward_tc_workspace_bytes": (c_size_t, [c_int64]),
+    "fem_mlp_backward_tc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                    c_size_t, c_void_p, c_void_p]),
     "fem_mlp_backward_workspace_bytes": (c_size_t, [c_int64]),
     "fem_mlp_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                  c_size_t, c_void_p]),

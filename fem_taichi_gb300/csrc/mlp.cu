@@ -18,9 +18,13 @@
 //                 clock) and sets an error flag on timeout; TMEM is always freed.
 //  * k_loss       per-node loss sum_r |C_i yhat_r - zhat_r|^2 over probe pairs (zhat ~ N(0,I),
 //                 yhat = G^{-1} K G^{-T} zhat) and its gradient w.r.t. the 6 outputs.
-//  * k_mlp_bwd    backward pass on CUDA cores (FP32): per 64-node tile, dZ and activations in
-//                 shared memory, register-tiled weight-gradient accumulation, one partial per
-//                 CTA; k_sum_partials reduces the partials in CTA order (deterministic).
+//  * k_mlp_bwd_tc backward pass on the tensor cores (the training default): dz1 = dz2 W2 and
+//                 the weight / bias gradients as tcgen05 products with BF16 operands and FP32
+//                 accumulation in TMEM (see the kernel's comment); one partial per CTA.
+//  * k_mlp_bwd    backward pass on CUDA cores in FP32 (no BF16 rounding of the gradients), kept
+//                 as the full-precision reference: per 64-node tile, register-tiled weight
+//                 gradients, one partial per CTA.  k_sum_partials reduces the partials of
+//                 either kernel in CTA order (deterministic).
 //  * k_adam       Adam on FP32 master weights + BF16 copies for the forward kernel.
 //  * k_learned_blocks  P_i = G_i^{-T} C_i G_i^{-1} in FP64 for the PCG.
 #include <cuda_bf16.h>
@@ -645,6 +649,240 @@ __global__ void __launch_bounds__(256) k_mlp_bwd(const BwdParams p) {
     if (tid < kOut - kOutUsed) out[ob3 + kOutUsed + tid] = 0.f;
 }
 
+// ---- backward on the tensor cores -------------------------------------------------------------
+//
+// k_mlp_bwd_tc: one persistent CTA of 128 threads per SM, 128 nodes per tile (thread = node).
+//  1. CUDA cores: h1 = bf16(silu(z1)), h2 = bf16(silu(z2)), s' = silu'(z), dz3 = dout[:6],
+//     dz2 = (dz3 W3[:6]) * s2' (K = 6 is too short for an MMA).
+//  2. tcgen05 (M = 128 nodes, N = 64, K = 64): D1 = bf16(dz2) W2 in TMEM columns [0, 64);
+//     the epilogue forms dz1 = D1 * s1'.
+//  3. tcgen05 gradient products, accumulated in TMEM across all tiles of the CTA:
+//       D_g  = [bf16(dz2)^T ; bf16(dz1)^T] (128 x K=nodes) . [h1 | X | valid]  (N = 96)
+//            -> rows 0-63: gW2 (cols 0-63) and gb2 (col 80); rows 64-127: gW1 (cols 64-79)
+//               and gb1 (col 80)                                      TMEM columns [64, 160)
+//       D_3  = [h2^T ; valid ; 0] (128 x K=nodes) . bf16(dz3)  (N = 16)
+//            -> rows 0-63: gW3^T (cols 0-5); row 64: gb3                TMEM columns [160, 176)
+//     The node dimension is K; each operand is written transposed into the no-swizzle
+//     K-major core-matrix layout by the thread that owns the node.
+//  4. After the last tile the accumulators are read back (tcgen05.ld) into this CTA's partial
+//     gradient, reduced in CTA order by k_sum_partials (deterministic).
+// BF16 operands, FP32 accumulation: the rounding points are dz3, dz2 and dz1 (as
+// mlp_oracle.backward_bf16 states them).  Every mbarrier wait is bounded and TMEM is freed on
+// every exit.
+constexpr int kBwdCols = 256;  // TMEM columns allocated (176 used)
+
+struct BwdTcParams {
+    const float* W;      // FP32 master parameters (flat)
+    const uint16_t* X;   // [n][16] bf16
+    const float* z1;     // [n][64]
+    const float* z2;     // [n][64]
+    const float* dout;   // [n][16]
+    int64_t n;
+    float* part;         // [gridDim][kNParams]
+    int* err;
+};
+
+struct BwdTcSmem {
+    alignas(1024) unsigned char Ag[kTile * kTile * 2];     // 32 KB [dz2^T ; dz1^T], K = 128 nodes
+    alignas(1024) unsigned char Bg[96 * kTile * 2];        // 24 KB [h1^T ; X^T ; valid ; 0]
+    alignas(1024) unsigned char A3[kTile * kTile * 2];     // 32 KB [h2^T ; valid ; 0]
+    alignas(1024) unsigned char B3[16 * kTile * 2];        // 4 KB  [dz3^T ; 0]
+    alignas(1024) unsigned char Dz2[kTile * kHid * 2];     // 16 KB dz2, node-major (A of D1)
+    alignas(1024) unsigned char W2T[kHid * kHid * 2];      // 8 KB  W2^T as B of D1 (row k, K = o)
+    float W3[kOutUsed][kHid];
+    alignas(8) uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ void put_bf16(unsigned char* tile, int row, int k, int K, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(tile + core_off(row, k, K)) = __float2bfloat16_rn(v);
+}
+
+__global__ void __launch_bounds__(kTile, 1) k_mlp_bwd_tc(const BwdTcParams p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    BwdTcSmem& s = *reinterpret_cast<BwdTcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // W2^T in the core-matrix layout: element (row k, col o) = W2[o][k], BF16 as the forward used it
+    for (int i = tid; i < kHid * kHid; i += kTile) {
+        const int o = i / kHid, k = i % kHid;
+        put_bf16(s.W2T, k, o, kHid, p.W[oW2 + i]);
+    }
+    for (int i = tid; i < kOutUsed * kHid; i += kTile) s.W3[i / kHid][i % kHid] = bf16r(p.W[oW3 + i]);
+    // constant zero rows of the operands (rows 81-95 of Bg, 65-127 of A3, 6-15 of B3)
+    for (int i = tid; i < 15 * kTile; i += kTile) put_bf16(s.Bg, 81 + i / kTile, i % kTile, kTile, 0.f);
+    for (int i = tid; i < 63 * kTile; i += kTile) put_bf16(s.A3, 65 + i / kTile, i % kTile, kTile, 0.f);
+    for (int i = tid; i < 10 * kTile; i += kTile) put_bf16(s.B3, 6 + i / kTile, i % kTile, kTile, 0.f);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmem_base)),
+                     "r"(uint32_t(kBwdCols)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&s.mbar)), "r"(1u));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_proxy_async();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s.tmem_base;
+    const uint32_t lane_base = uint32_t(32 * warp) << 16;
+    const uint32_t id_d1 = idesc_bf16(kTile, kHid), id_g = idesc_bf16(kTile, 96), id_3 = idesc_bf16(kTile, 16);
+    const uint32_t aDz2 = smem_u32(s.Dz2), aW2T = smem_u32(s.W2T);
+    const uint32_t aAg = smem_u32(s.Ag), aBg = smem_u32(s.Bg), aA3 = smem_u32(s.A3), aB3 = smem_u32(s.B3);
+    uint32_t phase = 0;
+    bool ok = true;
+    bool first = true;
+
+    for (int64_t tile = blockIdx.x; tile * kTile < p.n && ok; tile += gridDim.x) {
+        const int64_t node = tile * kTile + tid;
+        const bool valid = node < p.n;
+        const int t = tid;  // column (K index) of this node in the transposed operands
+        float s1g[kHid];
+        {
+            // dz3 and dz2 = (dz3 W3) s2'; h2^T, X^T, valid; dz3^T
+            float d3[kOutUsed];
+#pragma unroll
+            for (int o = 0; o < kOutUsed; ++o) d3[o] = valid ? p.dout[node * kOut + o] : 0.f;
+#pragma unroll
+            for (int o = 0; o < kOutUsed; ++o) put_bf16(s.B3, o, t, kTile, d3[o]);
+#pragma unroll
+            for (int c0 = 0; c0 < kHid; c0 += 16) {
+                float a1v[16], a2v[16], v[16];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float4 u1 = make_float4(0.f, 0.f, 0.f, 0.f), u2 = u1;
+                    if (valid) {
+                        u1 = *reinterpret_cast<const float4*>(p.z1 + node * kHid + c0 + 4 * q);
+                        u2 = *reinterpret_cast<const float4*>(p.z2 + node * kHid + c0 + 4 * q);
+                    }
+                    a1v[4 * q] = u1.x, a1v[4 * q + 1] = u1.y, a1v[4 * q + 2] = u1.z, a1v[4 * q + 3] = u1.w;
+                    a2v[4 * q] = u2.x, a2v[4 * q + 1] = u2.y, a2v[4 * q + 2] = u2.z, a2v[4 * q + 3] = u2.w;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = c0 + j;
+                    float d = 0.f;
+#pragma unroll
+                    for (int o = 0; o < kOutUsed; ++o) d = fmaf(s.W3[o][c], d3[o], d);
+                    d = valid ? d * silu_grad(a2v[j]) : 0.f;
+                    v[j] = d;
+                    put_bf16(s.Ag, c, t, kTile, d);                            // dz2^T (rows 0-63)
+                    put_bf16(s.A3, c, t, kTile, valid ? silu(a2v[j]) : 0.f);  // h2^T
+                    put_bf16(s.Bg, c, t, kTile, valid ? silu(a1v[j]) : 0.f);  // h1^T
+                    s1g[c] = valid ? silu_grad(a1v[j]) : 0.f;
+                }
+                store_row_bf16(s.Dz2, tid, c0, kHid, v);                       // dz2, node-major
+            }
+            uint4 xa = make_uint4(0, 0, 0, 0), xb = make_uint4(0, 0, 0, 0);
+            if (valid) {
+                const uint4* src = reinterpret_cast<const uint4*>(p.X + node * kIn);
+                xa = src[0];
+                xb = src[1];
+            }
+            const uint16_t* xs = reinterpret_cast<const uint16_t*>(&xa);
+            const uint16_t* xt = reinterpret_cast<const uint16_t*>(&xb);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                *reinterpret_cast<uint16_t*>(s.Bg + core_off(64 + k, t, kTile)) = xs[k];
+                *reinterpret_cast<uint16_t*>(s.Bg + core_off(72 + k, t, kTile)) = xt[k];
+            }
+            put_bf16(s.Bg, 80, t, kTile, valid ? 1.f : 0.f);
+            put_bf16(s.A3, 64, t, kTile, valid ? 1.f : 0.f);
+        }
+        fence_proxy_async();
+        __syncthreads();
+        // ---- D1 = dz2 W2 (M = 128 nodes, N = 64, K = 64 in four K = 16 slices) ---------------
+        if (tid == 0) {
+            fence_after();
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ++ks)
+                mma_bf16(tmem, sdesc(aDz2 + 256 * ks, 128, 1024), sdesc(aW2T + 256 * ks, 128, 1024), id_d1,
+                         ks > 0 ? 1u : 0u);
+            mma_commit(&s.mbar);
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(&s.mbar, phase));
+        phase ^= 1;
+        if (!ok) break;
+        fence_after();
+        // dz1 = D1 s1'  -> rows 64-127 of Ag (transposed)
+#pragma unroll
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + lane_base + uint32_t(c0), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) put_bf16(s.Ag, 64 + c0 + j, t, kTile, v[j] * s1g[c0 + j]);
+        }
+        fence_before();
+        fence_proxy_async();
+        __syncthreads();
+        // ---- gradient products, accumulated over the tiles (K = 128 nodes, eight K = 16 slices)
+        if (tid == 0) {
+            fence_after();
+#pragma unroll
+            for (int ks = 0; ks < kTile / 16; ++ks) {
+                const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+                mma_bf16(tmem + 64, sdesc(aAg + 256 * ks, 128, 2048), sdesc(aBg + 256 * ks, 128, 2048), id_g, acc);
+                mma_bf16(tmem + 160, sdesc(aA3 + 256 * ks, 128, 2048), sdesc(aB3 + 256 * ks, 128, 2048), id_3, acc);
+            }
+            mma_commit(&s.mbar);
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(&s.mbar, phase));
+        phase ^= 1;
+        first = false;
+        if (!ok) break;
+        fence_after();
+    }
+
+    // ---- this CTA's partial gradient --------------------------------------------------------------
+    float* out = p.part + int64_t(blockIdx.x) * kNParams;
+    if (ok) {
+        const int r = tid;  // TMEM lane = row of the accumulators
+        if (first) {
+            // no tile: zero partial
+            for (int i = tid; i < kNParams; i += kTile) out[i] = 0.f;
+        } else {
+#pragma unroll
+            for (int c0 = 0; c0 < 96; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + lane_base + uint32_t(64 + c0), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = c0 + j;
+                    if (r < 64) {
+                        if (c < 64) out[oW2 + r * kHid + c] = v[j];
+                        else if (c == 80) out[ob2 + r] = v[j];
+                    } else {
+                        if (c >= 64 && c < 80) out[oW1 + (r - 64) * kIn + (c - 64)] = v[j];
+                        else if (c == 80) out[ob1 + (r - 64)] = v[j];
+                    }
+                }
+            }
+            {
+                float v[16];
+                tmem_ld16(tmem + lane_base + 160u, v);
+                if (r < 64) {
+#pragma unroll
+                    for (int o = 0; o < kOutUsed; ++o) out[oW3 + o * kHid + r] = v[o];
+                } else if (r == 64) {
+#pragma unroll
+                    for (int o = 0; o < kOutUsed; ++o) out[ob3 + o] = v[o];
+                }
+            }
+            for (int i = kOutUsed * kHid + tid; i < kOut * kHid; i += kTile) out[oW3 + i] = 0.f;
+            if (tid < kOut - kOutUsed) out[ob3 + kOutUsed + tid] = 0.f;
+        }
+    } else if (tid == 0) {
+        atomicExch(p.err, 1);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(uint32_t(kBwdCols)));
+}
+
 __global__ void k_sum_partials(const float* __restrict__ part, int nblocks, int count, float* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
@@ -809,6 +1047,39 @@ extern "C" int fem_mlp_backward(const float* params, const uint16_t* X, const fl
     FEM_CUDA(cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     k_mlp_bwd<<<g, 256, smem, st>>>(p);
     FEM_LAUNCH_CHECK("k_mlp_bwd");
+    k_sum_partials<<<(kNParams + 255) / 256, 256, 0, st>>>(static_cast<const float*>(workspace), g, kNParams, grad);
+    FEM_LAUNCH_CHECK("k_sum_partials");
+    return FEM_OK;
+}
+
+extern "C" size_t fem_mlp_backward_tc_workspace_bytes(int64_t n) {
+    int dev = 0, sms = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t tiles = (n + kTile - 1) / kTile;
+    const int64_t g = std::max<int64_t>(1, std::min<int64_t>(tiles, sms));
+    return size_t(g) * kNParams * sizeof(float);
+}
+
+extern "C" int fem_mlp_backward_tc(const float* params, const uint16_t* X, const float* z1, const float* z2,
+                                   const float* dout, int64_t n, float* grad, void* workspace, size_t workspace_bytes,
+                                   int* err, void* stream) {
+    FEM_REQUIRE(params && X && z1 && z2 && dout && grad && workspace && err && n > 0, "bad arguments");
+    FEM_REQUIRE(aligned16(X) && aligned16(z1) && aligned16(z2), "X, z1 and z2 must be 16-byte aligned");
+    int dev = 0, sms = 0;
+    FEM_CUDA(cudaGetDevice(&dev));
+    FEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t tiles = (n + kTile - 1) / kTile;
+    const int g = int(std::max<int64_t>(1, std::min<int64_t>(tiles, sms)));
+    if (workspace_bytes < size_t(g) * kNParams * sizeof(float)) {
+        set_error("workspace too small: need %zu bytes", size_t(g) * kNParams * sizeof(float));
+        return FEM_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    BwdTcParams p{params, X, z1, z2, dout, n, static_cast<float*>(workspace), err};
+    const size_t smem = sizeof(BwdTcSmem) + 1024;
+    FEM_CUDA(cudaFuncSetAttribute(k_mlp_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    k_mlp_bwd_tc<<<g, kTile, smem, st>>>(p);
+    FEM_LAUNCH_CHECK("k_mlp_bwd_tc");
     k_sum_partials<<<(kNParams + 255) / 256, 256, 0, st>>>(static_cast<const float*>(workspace), g, kNParams, grad);
     FEM_LAUNCH_CHECK("k_sum_partials");
     return FEM_OK;

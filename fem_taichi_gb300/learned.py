@@ -10,7 +10,9 @@ Training data are Gaussian probe vectors zhat ~ N(0, I) and their products
 yhat = G^{-1} K G^{-T} zhat generated by the assembled operator itself (BSR SpMM); the loss
 is mean_{i,r} |C_i yhat_ir - zhat_ir|^2, i.e. C should act as the inverse of the
 block-scaled operator on the probes.  Forward: ``fem_mlp_forward`` (tcgen05); backward:
-``fem_mlp_backward`` (CUDA cores, FP32, deterministic); optimiser: Adam on FP32 masters.
+``fem_mlp_backward_tc`` (tcgen05, BF16 operands, FP32 accumulation; ``backward(...,
+tensor_cores=False)`` runs the FP32 CUDA-core kernel ``fem_mlp_backward``); both reduce their
+per-CTA partials in a fixed order (deterministic); optimiser: Adam on FP32 masters.
 """
 from __future__ import annotations
 
@@ -146,9 +148,19 @@ class LearnedPreconditioner:
         loss = part[:npart.value].sum() / (n * data.R)
         return loss, dout
 
-    def backward(self, X, z1, z2, dout):
+    def backward(self, X, z1, z2, dout, tensor_cores=True):
         n = X.shape[0]
         grad = torch.empty(N_PARAMS, dtype=torch.float32, device=self.device)
+        if tensor_cores:
+            nb = int(self.lib.fem_mlp_backward_tc_workspace_bytes(n))
+            ws = torch.empty(nb, dtype=torch.uint8, device=self.device)
+            err = torch.zeros(1, dtype=torch.int32, device=self.device)
+            _lib.check(self.lib.fem_mlp_backward_tc(_dptr(self.params), _dptr(X), _dptr(z1), _dptr(z2), _dptr(dout),
+                                                    n, _dptr(grad), _dptr(ws), nb, _dptr(err), _stream(self.device)),
+                       "fem_mlp_backward_tc")
+            if int(err.item()):
+                raise _lib.FemError(_lib.FEM_ERR_CUDA, "tensor-core backward timed out waiting on its mbarrier")
+            return grad
         nb = int(self.lib.fem_mlp_backward_workspace_bytes(n))
         ws = torch.empty(nb, dtype=torch.uint8, device=self.device)
         _lib.check(self.lib.fem_mlp_backward(_dptr(self.params), _dptr(X), _dptr(z1), _dptr(z2), _dptr(dout), n,

@@ -103,7 +103,9 @@ typedef struct fem_mesh {
     const int32_t* ne_ptr;  /* [n_node+1] */
     const int32_t* ne_list; /* [8*n_elem] */
     const int32_t* ne_inv;  /* [8*n_elem] (fem_gather_map), needed by FEM_ALGO_DD assembly */
-    const uint8_t* slot_map; /* [8*n_elem][8] (fem_gather_map), needed by FEM_ALGO_DD assembly */
+    const uint8_t* slot_map; /* [8*n_elem][8] (fem_gather_map), needed by FEM_ALGO_DD assembly and by
+                                the FP64 lane-per-corner gather (without it the FP64 gather runs one
+                                lane per block slot, and fem_assemble_host cannot split it) */
 } fem_mesh;
 
 typedef struct fem_material {
@@ -112,8 +114,10 @@ typedef struct fem_material {
 } fem_material;
 
 #define FEM_ALGO_DD 0   /* element integrals and gather sums in double-float on the FP32 pipes
-                           (inputs split from FP64, outputs formed in FP64); the default */
-#define FEM_ALGO_FP64 1 /* the same two kernels in native FP64 arithmetic                       */
+                           (inputs split from FP64, outputs formed in FP64; ~48-bit significands,
+                           not FP64 arithmetic) */
+#define FEM_ALGO_FP64 1 /* the same two stages in native FP64 arithmetic, as the reference computes
+                           (ti.f64); the Python drop-in's default                                 */
 
 typedef struct fem_assembly_out {
     int k_layout;          /* FEM_LAYOUT_BSR or FEM_LAYOUT_CSR                            */
@@ -401,6 +405,14 @@ size_t fem_mlp_backward_workspace_bytes(int64_t n);
 /* Parameter gradient grad[nparams] (deterministic CTA-ordered reduction). */
 int fem_mlp_backward(const float* params, const uint16_t* X, const float* z1, const float* z2, const float* dout,
                      int64_t n, float* grad, void* workspace, size_t workspace_bytes, void* stream);
+/* The same gradient on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in TMEM):
+ * dz3, dz2 and dz1 are rounded to BF16 where they enter a matrix product.  workspace: one
+ * partial gradient per SM (fem_mlp_backward_tc_workspace_bytes); *err (device int) is set if a
+ * bounded wait on the tensor cores timed out.  X, z1, z2 16-byte aligned. */
+size_t fem_mlp_backward_tc_workspace_bytes(int64_t n);
+int fem_mlp_backward_tc(const float* params, const uint16_t* X, const float* z1, const float* z2,
+                        const float* dout, int64_t n, float* grad, void* workspace, size_t workspace_bytes,
+                        int* err, void* stream);
 /* Adam step on the FP32 parameters (step >= 1); refreshes the BF16 weight copies. */
 int fem_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1, float beta2,
                  float eps, uint16_t* W1, uint16_t* W2, uint16_t* W3, void* stream);

@@ -113,6 +113,25 @@ def backward(params, X, z1, z2, dout):
     return np.concatenate([(dz1.T @ X).ravel(), dz1.sum(0), (dz2.T @ h1).ravel(), dz2.sum(0), gW3.ravel(), gb3])
 
 
+def backward_bf16(params, X, z1, z2, dout):
+    """The parameter gradient with the rounding points of the tensor-core backward
+    (fem_mlp_backward_tc): dz3, dz2 = (dz3 W3) s2' and dz1 = (bf16(dz2) W2) s1' are rounded to
+    BF16 where they become matrix-product operands; sums are exact here (FP32 on the GPU)."""
+    W1, b1, W2, b2, W3, b3 = unpack(params)
+    W2r, W3r = bf16_round(W2), bf16_round(W3)
+    h1 = bf16_round(silu(z1))
+    h2 = bf16_round(silu(z2))
+    d3 = np.asarray(dout, dtype=np.float64)[:, :N_USED]
+    dz2 = bf16_round((d3 @ W3r[:N_USED]) * silu_grad(z2))
+    dz1 = bf16_round((dz2 @ W2r) * silu_grad(z1))
+    d3b = bf16_round(d3)
+    gW3 = np.zeros((N_OUT, N_HID))
+    gW3[:N_USED] = d3b.T @ h2
+    gb3 = np.zeros(N_OUT)
+    gb3[:N_USED] = d3b.sum(0)
+    return np.concatenate([(dz1.T @ X).ravel(), dz1.sum(0), (dz2.T @ h1).ravel(), dz2.sum(0), gW3.ravel(), gb3])
+
+
 def precond_blocks(out, ginv):
     """P = G^{-T} C G^{-1} with C = L L^T; ginv (n,3,3) lower-triangular."""
     L = lower(out)
