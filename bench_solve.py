@@ -296,18 +296,24 @@ def c5_system(device="cuda", nrhs=32, seed=5):
 def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, maxit=1000, block_variants=True):
     """32 right-hand sides on the slender twisted slab (condition number far beyond FP32
     refinement).  The reference is the FP64 multigrid solve refined on compensated residuals
-    to the FP64 floor, cross-checked on 4 columns by the same procedure with a differently
-    built hierarchy (theta 0.16, degree-3 Chebyshev).  Block-diagonal preconditioners are run
+    to the FP64 floor, cross-checked on 2 columns by the same procedure with a different
+    preconditioner (degree-3 instead of degree-2 Chebyshev smoothing).  Rows: the FP64
+    multigrid solve with compensated residuals (``fp64_amg_extra_residual``, 32 and 1 RHS; the
+    residual of this system floors near 5e-8, and only refinement on compensated residuals
+    brings the error below 1e-8) and with plain FP64 residuals (``fp64_amg``, which stops at
+    the floor with an error above 1e-8).  Block-diagonal preconditioners are run
     on the first right-hand side with an iteration cap and reported with the error they
     reach ("not converged in `maxit` iterations")."""
     S, Fm = c5_system(device, nrhs)
     amg = amg_setup(S)
-    H2 = S.amg_variant(theta=0.16, pre_degree=3, post_degree=3)
-    Ur, ref = reference_solution(S, F=Fm, precond="amg", check=H2, check_cols=[0, 1, 2, 3],
-                                 check_name="multigrid, theta 0.16, degree-3 Chebyshev")
+    H2 = S.amg_variant(pre_degree=3, post_degree=3)
+    Ur, ref = reference_solution(S, F=Fm, precond="amg", check=H2, check_cols=[0, 1],
+                                 check_name="multigrid with degree-3 Chebyshev smoothing")
     H2.close()
-    variants = [("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg")),
-                ("fp64_amg_extra_residual", dict(rtol=rtol, mixed=False, precond="amg", residual="extra")),
+    variants = [("fp64_amg_extra_residual", dict(rtol=rtol, mixed=False, precond="amg", residual="extra")),
+                ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg")),
+                ("fp64_amg_extra_residual_1rhs", dict(F=Fm[:, 0].contiguous(), rtol=rtol, mixed=False, precond="amg",
+                                                      residual="extra")),
                 ("fp64_amg_1rhs", dict(F=Fm[:, 0].contiguous(), rtol=rtol, mixed=False, precond="amg"))]
     rows = []
     for label, kw in variants:

@@ -2,17 +2,23 @@
 //
 // Two kernels, both deterministic and free of floating-point atomics:
 //
-//  1. k_hex8_element -- 8 threads per element.  Phase A: thread g handles Gauss point g
-//     (Jacobian, adjugate, determinant, the 8 scaled gradients R_a = dN_a/dxi . adj(J),
-//     and the centrifugal load density); results are staged in shared memory.  Phase B:
-//     the 36 node pairs (a <= b) are split across the 8 threads; each accumulates the
-//     Gram matrix P_ab = sum_g R_a R_b^T / det_g and turns it into the 3x3 stiffness
-//     block  K_ab[p][q] = lam P[p][q] + mu P[q][p],  K_ab[p][p] = D0d P[p][p] + mu (tr P - P[p][p]),
-//     which equals sum_g det (B1_a^T D0 B1_b + B2_a^T D1 B2_b) of the reference
-//     (FEM_model_bsr.py:262-274, 303-347) with a different summation order.  The
-//     consistent mass M_ab = DE sum_g det_g N_a N_b (FEM_model_bsr.py:276-287) and the
-//     centrifugal load F_a (FEM_model_bsr.py:229-245, 291-300) are produced alongside.
-//     Each element writes one 3 KB record: 36 x (K 3x3 + M) and 8 x F(3).
+//  1. k_hex8_element -- 8 threads per element.  Thread t first forms coefficient t of the
+//     element's trilinear map x(xi) = sum_k c_k m_k(xi) (m = 1, xi, eta, zeta, xi eta,
+//     eta zeta, xi zeta, xi eta zeta; c_k = 1/8 sum_a m_k(corner a) x_a) and W x_t, where W is
+//     the centrifugal operator of UnitVectorF (FEM_model_bsr.py:291-300).  Phase A: thread g
+//     handles Gauss point g (Jacobian from the coefficients, 27 FMA instead of 72; adjugate,
+//     determinant, the 8 scaled gradients R_a = dN_a/dxi . adj(J)); results are staged in
+//     shared memory.  Phase B: the 36 node pairs (a <= b) are split across the 8 threads;
+//     each accumulates the Gram matrix P_ab = sum_g R_a R_b^T / det_g and turns it into the
+//     3x3 stiffness block  K_ab[p][q] = lam P[p][q] + mu P[q][p],
+//     K_ab[p][p] = D0d P[p][p] + mu (tr P - P[p][p]), which equals sum_g det (B1_a^T D0 B1_b +
+//     B2_a^T D1 B2_b) of the reference (FEM_model_bsr.py:262-274, 303-347) with a different
+//     summation order.  The consistent mass M_ab = DE sum_g det_g N_a N_b
+//     (FEM_model_bsr.py:276-287) uses a table of N_a N_b at the Gauss points.  The centrifugal
+//     load (FEM_model_bsr.py:229-245) is F_a = sum_g DE det_g N_a(g) W x(g); W x is linear and
+//     the isoparametric map reproduces it at the Gauss points, W x(g) = sum_b N_b(g) W x_b, so
+//     F_a = sum_b M_ab W x_b: the same quantity from the mass blocks, with no per-Gauss-point
+//     load density.  Each element writes one 3 KB record: 36 x (K 3x3 + M) and 8 x F(3).
 //
 //  2. k_gather -- one warp per block row i.  Lane l owns slot l of the row (column node
 //     indices[indptr[i] + l]).  The warp walks the incident (element, corner) list of
@@ -42,7 +48,7 @@ struct ElemParams {
     int64_t e_begin, e_end;  // elements [e_begin, e_end) of this launch
     double* rec;
     double DE, D0d, lam, mu;
-    double w0, w1, w2;
+    double wc[3][3];   // centrifugal operator: f = wc . x (UnitVectorF)
     DevTables tab;
     double nn[36][8];  // N_a(g) N_b(g) for pair (a <= b), Gauss point g
 };
@@ -52,11 +58,24 @@ struct ElemSmem {
     double nr[8][8];
     double nn[36][8];
     double x[kEpc][8][3];
+    double xl[kEpc][8][3];      // corner coordinates relative to corner 0
+    double cf[kEpc][8][3];      // trilinear coefficients c_k of the element map (c_0 unused)
+    double wx[kEpc][8][3];      // W x_a: centrifugal density per unit mass at corner a
     double R[kEpc][8][kRPad];   // R_a(g)[i] at [el][g][3a+i]
     double Rs[kEpc][8][kRPad];  // R_a(g)[i] / det_g
     double det[kEpc][8];
-    double c[kEpc][8][3];       // DE * det_g * f(x(g))
+    double m[kEpc][36];         // M_ab of the element (DE included)
 };
+
+// m_k(corner a) for the trilinear monomials 1, xi, eta, zeta, xi eta, eta zeta, xi zeta,
+// xi eta zeta; corner signs in the reference's node order (FEM_model_bsr.py:371-382):
+// xi < 0 at corners 1, 2, 5, 6 (mask 0x66), eta < 0 at 2, 3, 6, 7 (0xCC), zeta < 0 at 0-3
+// (0x0F); monomial k contains xi for k in {1, 4, 6, 7} (0xD2), eta for {2, 4, 5, 7} (0xB4),
+// zeta for {3, 5, 6, 7} (0xE8).
+__device__ __forceinline__ double monomial_sign(int k, int a) {
+    const int neg = (((0xD2 >> k) & (0x66 >> a)) ^ ((0xB4 >> k) & (0xCC >> a)) ^ ((0xE8 >> k) & (0x0F >> a))) & 1;
+    return neg ? -1.0 : 1.0;
+}
 
 // Off-diagonal pair list (a < b), 28 entries; thread t takes entries t, t+8, t+16, t+24.
 __device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
@@ -91,19 +110,40 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
     }
     __syncthreads();
 
+    // ---- coefficient t of the trilinear map, and W x_t ---------------------------------
+    if (valid) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s.wx[el][t][i] = p.wc[i][0] * s.x[el][t][0] + p.wc[i][1] * s.x[el][t][1] + p.wc[i][2] * s.x[el][t][2];
+            s.xl[el][t][i] = s.x[el][t][i] - s.x[el][0][i];   // element-local: no offset to cancel
+        }
+    }
+    __syncthreads();
+    if (valid) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int a = 1; a < 8; ++a) acc = fma(monomial_sign(t, a), s.xl[el][a][i], acc);
+            s.cf[el][t][i] = 0.125 * acc;
+        }
+    }
+    __syncthreads();
+
     // ---- phase A: Gauss point g = t ------------------------------------------------
     if (valid) {
         const int g = t;
+        // Gauss point coordinates in the reference's order (zeta fastest, FEM_model_bsr.py:425-432)
+        const double xi = (g & 4) ? kGS1 : -kGS1, et = (g & 2) ? kGS1 : -kGS1, ze = (g & 1) ? kGS1 : -kGS1;
         double J[3][3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                double acc = 0.0;
-#pragma unroll
-                for (int a = 0; a < 8; ++a) acc = fma(s.x[el][a][i], s.dnr[g][a][d], acc);
-                J[i][d] = acc;
-            }
+        for (int i = 0; i < 3; ++i) {
+            const double c1 = s.cf[el][1][i], c2 = s.cf[el][2][i], c3 = s.cf[el][3][i], c4 = s.cf[el][4][i];
+            const double c5 = s.cf[el][5][i], c6 = s.cf[el][6][i], c7 = s.cf[el][7][i];
+            J[i][0] = fma(ze, fma(et, c7, c6), fma(et, c4, c1));   // dx/dxi
+            J[i][1] = fma(ze, fma(xi, c7, c5), fma(xi, c4, c2));   // dx/deta
+            J[i][2] = fma(et, fma(xi, c7, c5), fma(xi, c6, c3));   // dx/dzeta
+        }
         double A[3][3];  // adjugate: inverse(J) = A / det
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -123,31 +163,14 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
                 s.Rs[el][g][3 * a + i] = r * inv;
             }
         s.det[el][g] = det;
-        double X[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            double acc = 0.0;
-#pragma unroll
-            for (int a = 0; a < 8; ++a) acc = fma(s.nr[g][a], s.x[el][a][i], acc);
-            X[i] = acc;
-        }
-        const double w0 = p.w0, w1 = p.w1, w2 = p.w2;
-        const double f0 = w1 * w1 * X[0] + w2 * w2 * X[0] - w0 * w1 * X[1] - w0 * w2 * X[2];
-        const double f1 = w0 * w0 * X[1] + w2 * w2 * X[1] - w1 * w2 * X[2] - w1 * w0 * X[0];
-        const double f2 = w1 * w1 * X[2] + w0 * w0 * X[2] - w2 * w0 * X[0] - w2 * w1 * X[1];
-        const double jd = p.DE * det;
-        s.c[el][g][0] = jd * f0;
-        s.c[el][g][1] = jd * f1;
-        s.c[el][g][2] = jd * f2;
     }
     __syncthreads();
-    if (!valid) return;
 
     // ---- phase B: node pairs -----------------------------------------------------------
-    double* rec = p.rec + e * kRec;
+    double* rec = p.rec + (valid ? e : 0) * kRec;
     const double lam = p.lam, mu = p.mu, D0d = p.D0d, DE = p.DE;
     // diagonal pair (t, t): P symmetric
-    {
+    if (valid) {
         const int a = t, pi = pair_index(a, a);
         double P00 = 0, P11 = 0, P22 = 0, P01 = 0, P02 = 0, P12 = 0, m = 0;
 #pragma unroll
@@ -171,9 +194,10 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
         o[2] = o[6] = lm * P02;
         o[5] = o[7] = lm * P12;
         o[9] = DE * m;
+        s.m[el][pi] = o[9];
     }
     // off-diagonal pairs
-    for (int q = t; q < 28; q += 8) {
+    for (int q = t; q < 28 && valid; q += 8) {
         int a, b;
         offdiag_pair(q, a, b);
         const int pi = pair_index(a, b);
@@ -205,16 +229,19 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
         o[6] = lam * P[2][0] + mu * P[0][2];
         o[7] = lam * P[2][1] + mu * P[1][2];
         o[9] = DE * m;
+        s.m[el][pi] = o[9];
     }
-    // element load for corner t
-    {
+    // element load for corner t: F_t = sum_b M_tb W x_b (the mass blocks of the other threads'
+    // pairs come through shared memory)
+    __syncthreads();
+    if (valid) {
         double f0 = 0, f1 = 0, f2 = 0;
 #pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            const double n = s.nr[g][t];
-            f0 = fma(n, s.c[el][g][0], f0);
-            f1 = fma(n, s.c[el][g][1], f1);
-            f2 = fma(n, s.c[el][g][2], f2);
+        for (int b = 0; b < 8; ++b) {
+            const double mv = s.m[el][pair_index(min(t, b), max(t, b))];
+            f0 = fma(mv, s.wx[el][b][0], f0);
+            f1 = fma(mv, s.wx[el][b][1], f1);
+            f2 = fma(mv, s.wx[el][b][2], f2);
         }
         rec[kFOff + 3 * t + 0] = f0;
         rec[kFOff + 3 * t + 1] = f1;
@@ -683,9 +710,14 @@ int launch_hex8_element(const fem_mesh* mesh, const fem_material* mat, void* wor
     ep.D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // FEM_model_bsr.py:435-437
     ep.lam = EX * PO / (1 + PO) / (1 - 2 * PO);         // :439-445
     ep.mu = EX / 2 / (1 + PO);                          // :447-449
-    ep.w0 = mat->omega[0];
-    ep.w1 = mat->omega[1];
-    ep.w2 = mat->omega[2];
+    {
+        const double w0 = mat->omega[0], w1 = mat->omega[1], w2 = mat->omega[2];
+        const double wc[3][3] = {{w1 * w1 + w2 * w2, -w0 * w1, -w0 * w2},   // UnitVectorF, FEM_model_bsr.py:291-300
+                                 {-w1 * w0, w0 * w0 + w2 * w2, -w1 * w2},
+                                 {-w2 * w0, -w2 * w1, w1 * w1 + w0 * w0}};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) ep.wc[i][j] = wc[i][j];
+    }
     ep.tab = make_tables();
     const ShapeTables& T = shape_tables();
     for (int a = 0; a < 8; ++a)

@@ -1,6 +1,10 @@
 // Nodal stress recovery for sm_103a (POST_process.py:72-99, 172-223).
 //
-//  1. k_stress_element -- 8 threads per element.  Thread g evaluates the displacement
+//  1. k_stress_element -- 8 threads per element.  Thread t first forms coefficient t of the
+//     trilinear interpolants of the element-local coordinates and of the displacements
+//     (c_k = 1/8 sum_a m_k(corner a) v_a for the monomials 1, xi, eta, zeta, xi eta, eta zeta,
+//     xi zeta, xi eta zeta), so that J and dU/dxi at a Gauss point cost 27 FMA each instead
+//     of 72.  Thread g then evaluates the displacement
 //     gradient at Gauss point g as H = (sum_a u_a (x) dN_a/dxi) . adj(J) / det, and the
 //     stresses  sigma_n = D0 (H00, H11, H22),  sigma_s = mu (H01+H10, H12+H21, H02+H20)
 //     (components xy, yz, xz as UnitVectorS orders them, POST_process.py:190-209).
@@ -30,17 +34,35 @@ struct StressParams {
     int64_t n_elem;
     double* rec;  // [n_elem][8][6]
     double D0d, lam, mu;
-    DevTables tab;
     double W[8][8];
 };
 
 struct StressSmem {
-    double dnr[8][8][3];
     double W[8][8];
     double x[kEpc][8][3];
     double u[kEpc][8][3];
+    double cx[kEpc][8][3];  // trilinear coefficients of the element-local coordinates
+    double cu[kEpc][8][3];  // and of the displacements
     double sv[kEpc][8][kSvPad];
 };
+
+// m_k(corner a) of the trilinear monomials (1, xi, eta, zeta, xi eta, eta zeta, xi zeta,
+// xi eta zeta) at the reference's corner order (POST_process.py:238-273): xi < 0 at corners
+// 1, 2, 5, 6 (0x66), eta < 0 at 2, 3, 6, 7 (0xCC), zeta < 0 at 0-3 (0x0F); monomial k holds
+// xi for k in {1, 4, 6, 7} (0xD2), eta for {2, 4, 5, 7} (0xB4), zeta for {3, 5, 6, 7} (0xE8).
+__device__ __forceinline__ double monomial_sign(int k, int a) {
+    const int neg = (((0xD2 >> k) & (0x66 >> a)) ^ ((0xB4 >> k) & (0xCC >> a)) ^ ((0xE8 >> k) & (0x0F >> a))) & 1;
+    return neg ? -1.0 : 1.0;
+}
+
+// d/dxi, d/deta, d/dzeta of sum_k c_k m_k at (xi, eta, zeta) for one component
+__device__ __forceinline__ void trilinear_grad(const double (*c)[3], int i, double xi, double et, double ze,
+                                               double& d0, double& d1, double& d2) {
+    const double c1 = c[1][i], c2 = c[2][i], c3 = c[3][i], c4 = c[4][i], c5 = c[5][i], c6 = c[6][i], c7 = c[7][i];
+    d0 = fma(ze, fma(et, c7, c6), fma(et, c4, c1));
+    d1 = fma(ze, fma(xi, c7, c5), fma(xi, c4, c2));
+    d2 = fma(et, fma(xi, c7, c5), fma(xi, c6, c3));
+}
 
 __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams p) {
     __shared__ StressSmem s;
@@ -49,7 +71,6 @@ __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams 
     const int t = tid & 7;
     const int64_t e = int64_t(blockIdx.x) * kEpc + el;
     const bool valid = e < p.n_elem;
-    for (int k = tid; k < 8 * 8 * 3; k += kThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
     for (int k = tid; k < 64; k += kThreads) (&s.W[0][0])[k] = (&p.W[0][0])[k];
     if (valid) {
         const int node = __ldg(reinterpret_cast<const int*>(p.conn4) + 8 * e + t);
@@ -60,22 +81,46 @@ __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams 
         }
     }
     __syncthreads();
+    // element-local values (corner 0 subtracted; the gradients depend on differences only)
+    double x0[3] = {0, 0, 0}, u0[3] = {0, 0, 0};
+    if (valid) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) x0[i] = s.x[el][0][i], u0[i] = s.u[el][0][i];
+    }
+    __syncthreads();
+    if (valid) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s.x[el][t][i] -= x0[i];
+            s.u[el][t][i] -= u0[i];
+        }
+    }
+    __syncthreads();
+    if (valid) {
+        // coefficient t of the interpolants (corner 0 is now zero)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double ax = 0.0, au = 0.0;
+#pragma unroll
+            for (int a = 1; a < 8; ++a) {
+                const double m = monomial_sign(t, a);
+                ax = fma(m, s.x[el][a][i], ax);
+                au = fma(m, s.u[el][a][i], au);
+            }
+            s.cx[el][t][i] = 0.125 * ax;
+            s.cu[el][t][i] = 0.125 * au;
+        }
+    }
+    __syncthreads();
     if (valid) {
         const int g = t;
+        const double xi = (g & 4) ? kGS1 : -kGS1, et = (g & 2) ? kGS1 : -kGS1, ze = (g & 1) ? kGS1 : -kGS1;
         double J[3][3], G[3][3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                double aj = 0.0, ag = 0.0;
-#pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    aj = fma(s.x[el][a][i], s.dnr[g][a][d], aj);
-                    ag = fma(s.u[el][a][i], s.dnr[g][a][d], ag);
-                }
-                J[i][d] = aj;
-                G[i][d] = ag;
-            }
+        for (int i = 0; i < 3; ++i) {
+            trilinear_grad(s.cx[el], i, xi, et, ze, J[i][0], J[i][1], J[i][2]);
+            trilinear_grad(s.cu[el], i, xi, et, ze, G[i][0], G[i][1], G[i][2]);
+        }
         double A[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -230,7 +275,6 @@ extern "C" int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, cons
         sp.D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // POST_process.py:292-302
         sp.lam = EX * PO / (1 + PO) / (1 - 2 * PO);
         sp.mu = EX / 2 / (1 + PO);                          // :304-306
-        sp.tab = make_tables();
         for (int j = 0; j < 8; ++j)
             for (int k = 0; k < 8; ++k) sp.W[j][k] = extrap[8 * j + k];
         const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
@@ -246,7 +290,7 @@ extern "C" int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, cons
 
 extern "C" int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u, const int32_t* co_elem,
                           const double* extrap, double* out, void* workspace, size_t workspace_bytes, void* stream) {
-    return fem_stress_ex(mesh, mat, u, co_elem, extrap, out, workspace, workspace_bytes, FEM_ALGO_DD, stream);
+    return fem_stress_ex(mesh, mat, u, co_elem, extrap, out, workspace, workspace_bytes, FEM_ALGO_FP64, stream);
 }
 
 // ---- allocation-free variant ------------------------------------------------------------------
@@ -299,7 +343,7 @@ extern "C" int fem_stress_noalloc(const fem_mesh* mesh, const fem_material* mat,
     return fem_stress(mesh, mat, u, co_elem, extrap, out, scratch, sizeof(g_stress_scratch), stream);
 }
 
-// ---- double-float variant (FEM_ALGO_DD, the default of fem_stress) -----------------------------
+// ---- double-float variant (FEM_ALGO_DD; fem_stress runs FEM_ALGO_FP64) ----------------------------
 // Same two kernels and record size as above, with the FP64 arithmetic moved to double-float
 // on the FP32 pipes (fem_dd.cuh): node coordinates and displacements are made element-local
 // in FP64 first (the gradient only depends on differences), the corner values are stored as

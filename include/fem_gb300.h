@@ -188,7 +188,8 @@ int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* r
 /* ---- stress recovery ------------------------------------------------------------- */
 /* u: [n_node][3] displacement; co_elem: [n_node]; extrap: HOST [8][8] weights W[j][k]
  * (node j <- Gauss point k; POST_process.py:176-181); out: [n_node][10] =
- * [xx,yy,zz,xy,yz,xz, p1>=p2>=p3, "VM" as written at POST_process.py:93-94]. */
+ * [xx,yy,zz,xy,yz,xz, p1>=p2>=p3, "VM" as written at POST_process.py:93-94].
+ * fem_stress computes in FP64 (FEM_ALGO_FP64); fem_stress_ex takes the algo. */
 size_t fem_stress_workspace_bytes(int64_t n_elem);
 int fem_stress(const fem_mesh* mesh, const fem_material* mat, const double* u,
                const int32_t* co_elem, const double* extrap, double* out, void* workspace,
