@@ -47,14 +47,17 @@ METRIC = "K+M assembly Melem/s"
 UNIT = "Melem/s"
 
 # FP64 operations of one element's integrals (FMA = 2), counted from k_hex8_element:
-# phase A per Gauss point: J 72 FMA, adjugate 18, det 3, reciprocal ~10, R 72 (24x3),
-# R/det 24, load density ~40; phase B: 28 off-diagonal pairs x (72 + 4 + 21 + 1) +
-# 8 diagonal pairs x (48 + 8 + 14) + F 192.
-ELEM_FP64_FLOPS = 2 * 8 * (72 + 72 + 24) + 8 * (18 + 3 + 10 + 40) + 28 * (2 * 76 + 21 + 1) + 8 * (2 * 56 + 14) + 2 * 192
-# FP64 operations of one element of the stress element kernel (k_stress_element): per Gauss
-# point J and the displacement gradient 144 FMA, adjugate 27, det 5, reciprocal ~10, H 63,
+# W x and element-local coordinates 8 x (15 + 3); trilinear coefficients 24 x 15;
+# per Gauss point J 27 FMA, adjugate 27, det 5, reciprocal ~10, R 24 x 5, R/det 24;
+# 8 diagonal pairs x (8 x 7 FMA + 17); 28 off-diagonal pairs x (8 x 10 FMA + 31);
+# F = M W x 8 x 24 FMA.  ELEM_FP64_INSTR counts instructions (FMA = 1) the same way.
+ELEM_FP64_FLOPS = 8 * 18 + 24 * 15 + 8 * (54 + 27 + 5 + 10 + 120 + 24) + 8 * (112 + 17) + 28 * (160 + 31) + 8 * 48
+ELEM_FP64_INSTR = 8 * 12 + 24 * 8 + 8 * (27 + 18 + 3 + 5 + 72 + 24) + 8 * (56 + 15) + 28 * (80 + 22) + 8 * 24
+# FP64 operations of one element of the stress element kernel (k_stress_element): corner 0
+# subtracted 48; trilinear coefficients of x and u 24 x 2 x (7 FMA + 1); per Gauss point J
+# and the displacement gradient 2 x 27 FMA, adjugate 27, det 5, reciprocal ~10, H 9 x 6,
 # stresses 18; extrapolation to the 8 corners 8 x 6 x 8 FMA.
-STRESS_ELEM_FP64_FLOPS = 8 * (2 * 144 + 27 + 5 + 10 + 63 + 18) + 2 * 8 * 6 * 8
+STRESS_ELEM_FP64_FLOPS = 48 + 24 * 2 * 15 + 8 * (2 * 54 + 27 + 5 + 10 + 54 + 18) + 2 * 8 * 6 * 8
 
 
 def parse():
@@ -408,6 +411,8 @@ def main():
                                   "achieved_tflops": fp64_ach, "peak_tflops": fp64_peak,
                                   "peak_kind": "measured FP64 FMA rate of this device (fem_probe_fma_tflops)",
                                   "frac_fp64": fp64_ach / fp64_peak,
+                                  "instr_per_elem": ELEM_FP64_INSTR,
+                                  "frac_fp64_instr": E * ELEM_FP64_INSTR / (el_ms * 1e-3) / (fp64_peak * 1e12 / 2),
                                   "element_share": el_ms / (el_ms + ga_ms)}},
             "kernels": {"k_hex8_element_ms": el_ms, "k_gather_ms": ga_ms,
                         "share_element": el_ms / (el_ms + ga_ms), "share_gather": ga_ms / (el_ms + ga_ms)},

@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from fem_taichi_gb300 import mesh as _mesh
-from fem_taichi_gb300.learned import LearnedPreconditioner, NodeData
+from fem_taichi_gb300.learned import LearnedPreconditioner, LearnedSmoother, NodeData
 from fem_taichi_gb300.model import Model
 from fem_taichi_gb300.solve import DeviceSystem
 
@@ -83,6 +83,37 @@ def train_c4(count=50, steps=300, lr=3e-3, n_probes=8, seed=0, device="cuda", mi
                  "loss_end": hist[-1], "data_s": t_data, "train_s": t_train}
 
 
+def smoother_cases(count=10, seed=0, device="cuda", min_nodes=8_000, max_nodes=60_000):
+    """Training cases of the learned smoother: (system, device multigrid hierarchy, seeded
+    random right-hand side) on blocks of the c4 training family."""
+    cases = []
+    for k, (P, mat) in enumerate(training_meshes(count, seed, min_nodes=min_nodes, max_nodes=max_nodes)):
+        S = DeviceSystem(Model(P.name, P, mat, device=device))
+        H = S.amg_variant()
+        g = torch.Generator(device=S.device).manual_seed(100 + k)
+        F = torch.randn(S.F.shape, generator=g, device=S.device, dtype=torch.float64)
+        cases.append((S, H, F))
+    return cases
+
+
+def train_smoother(count=10, seed=0, device="cuda", iters=12, **kw):
+    """Learned per-level Chebyshev smoother weights (learned.py:LearnedSmoother) fitted on
+    the c4 training family; returns (smoother, info)."""
+    t0 = time.perf_counter()
+    cases = smoother_cases(count, seed, device, **kw)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    sm = LearnedSmoother()
+    t1 = time.perf_counter()
+    l0, l1 = sm.fit(cases, iters=iters)
+    t_train = time.perf_counter() - t1
+    for _, H, _ in cases:
+        H.close()
+    return sm, {"meshes": count, "nodes": int(sum(S.n for S, _, _ in cases)), "iters": iters,
+                "loss_start": l0, "loss_end": l1, "evaluations": len(sm.history), "data_s": t_data,
+                "train_s": t_train, "weights": sm.state_dict()}
+
+
 def reference_solution(S: DeviceSystem, F=None, precond="amg", check=None, check_cols=None, check_name=None):
     """FP64 reference solution standing in for the reference's Pardiso (SOLVE_static.py:31-33):
     FP64 PCG followed by residual-replacement refinement on compensated (twice-FP64-accurate)
@@ -108,16 +139,33 @@ def reference_solution(S: DeviceSystem, F=None, precond="amg", check=None, check
     return U1, out
 
 
-def amg_setup(S: DeviceSystem, **opts):
-    """Builds the multigrid hierarchy of S (host setup + upload) and reports its cost."""
+def _levels(H):
+    return [(l["n"], l["b"], l["nnzb_A"] or None) for l in H.levels()]
+
+
+def amg_setup(S: DeviceSystem, compare_host=False, **opts):
+    """Builds the multigrid hierarchy of S on the device and reports its cost; with
+    compare_host, also the cost of the host setup of the same hierarchy (copy of K to the
+    host, setup, upload)."""
+    torch.cuda.synchronize()
     t = time.perf_counter()
     H = S.amg(**opts)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t
     lv = H.levels()
-    return {"setup_s": H.setup_s, "upload_s": H.upload_s, "wall_s": wall, "phases_s": H.setup_phases(),
-            "levels": [(l["n"], l["b"], l["nnzb_A"] or None) for l in lv],
-            "operator_complexity": (S.nnzb * 9 + sum(l["nnzb_A"] * 36 for l in lv[1:])) / (S.nnzb * 9)}
+    out = {"where": H.where, "setup_s": H.setup_s, "upload_s": H.upload_s, "wall_s": wall,
+           "phases_s": H.setup_phases(), "levels": _levels(H),
+           "operator_complexity": (S.nnzb * 9 + sum(l["nnzb_A"] * 36 for l in lv[1:])) / (S.nnzb * 9)}
+    if compare_host:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        Hh = S.amg_variant(setup="host", **opts)
+        torch.cuda.synchronize()
+        out["host_setup"] = {"wall_s": time.perf_counter() - t, "setup_s": Hh.setup_s, "upload_s": Hh.upload_s,
+                             "phases_s": Hh.setup_phases(), "levels": _levels(Hh),
+                             "same_levels": _levels(Hh) == out["levels"]}
+        Hh.close()
+    return out
 
 
 def relerr(U, Ur):
@@ -245,7 +293,7 @@ def face_rhs(S: DeviceSystem, P, F0, nrhs, face, seed):
     return Fm
 
 
-def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32):
+def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32, smoother=None):
     """Learned preconditioner on the unseen 160x160x20 block: 1 and 32 right-hand sides
     (the top traction plus 31 seeded random top-face loads), learned vs plain block Jacobi,
     against the FP64 reference."""
@@ -275,6 +323,17 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32):
                              ("mixed_bj_32rhs", dict(rtol=rtol, mixed=True)),
                              ("mixed_learned_32rhs", dict(rtol=rtol, mixed=True, precond=Pl)),
                              ("fp64_amg_32rhs", dict(rtol=rtol, mixed=False, precond="amg"))], F=Fm, amg=amg)
+    # learned smoother weights (trained on the same family) in a second hierarchy of K
+    sm_info = {}
+    if smoother is None:
+        smoother, sm_info = train_smoother(device=device)
+    Hl = smoother.apply(S.amg_variant())
+    for F_, Ur_, suffix in ((F1, Ur, ""), (Fm, Urm, "_32rhs")):
+        r = compare(S, Ur_, [("fp64_amg_learned_smoother" + suffix, dict(rtol=rtol, mixed=False, precond=Hl))],
+                    F=F_)[0]
+        r["setup_s"] = amg["wall_s"]
+        rows.append(r)
+    Hl.close()
     by = {r["label"]: r for r in rows}
     gain = {}
     for suffix in ("", "_32rhs"):
@@ -282,8 +341,12 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32):
         gain["learned_vs_mixed_bj" + suffix] = {"iterations": lb["iterations"] / max(bj["iterations"], 1),
                                                "wall": lb["wall_s"] / bj["wall_s"]}
         gain["learned_mixed_vs_fp64_bj" + suffix] = {"wall": lb["wall_s"] / fb["wall_s"]}
+        ls, da = by["fp64_amg_learned_smoother" + suffix], by["fp64_amg" + suffix]
+        gain["learned_smoother_vs_amg" + suffix] = {"iterations": ls["iterations"] / max(da["iterations"], 1),
+                                                   "wall": ls["wall_s"] / da["wall_s"]}
     return {"workload": "c4 eval 160x160x20, 544,341 nodes, 1 and %d RHS" % nrhs, "training": info,
-            "inference_s": t_inf, "reference": ref, "solves": rows, "amg": amg, "gain": gain}, net
+            "smoother_training": sm_info, "inference_s": t_inf, "reference": ref, "solves": rows, "amg": amg,
+            "gain": gain}, net
 
 
 def c5_system(device="cuda", nrhs=32, seed=5):
@@ -305,7 +368,7 @@ def c5_study(net=None, device="cuda", rtol=1e-10, nrhs=32, include_fp64=True, ma
     on the first right-hand side with an iteration cap and reported with the error they
     reach ("not converged in `maxit` iterations")."""
     S, Fm = c5_system(device, nrhs)
-    amg = amg_setup(S)
+    amg = amg_setup(S, compare_host=True)
     H2 = S.amg_variant(pre_degree=3, post_degree=3)
     Ur, ref = reference_solution(S, F=Fm, precond="amg", check=H2, check_cols=[0, 1],
                                  check_name="multigrid with degree-3 Chebyshev smoothing")

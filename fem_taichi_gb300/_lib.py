@@ -141,9 +141,12 @@ SIGNATURES = {
     "fem_amg_default_opts": (None, [ctypes.POINTER(FemAmgOpts)]),
     "fem_amg_setup": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(FemAmgOpts),
                               ctypes.POINTER(c_void_p)]),
+    "fem_amg_setup_device": (c_int, [ctypes.POINTER(FemBsr), c_void_p, c_void_p, c_void_p, ctypes.POINTER(FemAmgOpts),
+                                     c_void_p, ctypes.POINTER(c_void_p)]),
     "fem_amg_upload": (c_int, [c_void_p, c_void_p]),
     "fem_amg_destroy": (None, [c_void_p]),
     "fem_amg_num_levels": (c_int, [c_void_p]),
+    "fem_amg_set_smoother": (c_int, [c_void_p, c_int, ctypes.c_double, ctypes.c_double]),
     "fem_amg_setup_phases": (c_int, [c_void_p, c_void_p]),
     "fem_amg_get_level": (c_int, [c_void_p, c_int, ctypes.POINTER(FemAmgLevelInfo)]),
     "fem_amg_export": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -161,6 +164,11 @@ SIGNATURES = {
                                 c_void_p]),
     "fem_mlp_loss_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int64, c_void_p, c_void_p,
                                   ctypes.POINTER(c_int), c_void_p]),
+    "fem_ts_gemm_tn_workspace_bytes": (c_size_t, [c_int64, c_int, c_int]),
+    "fem_ts_gemm_tn": (c_int, [c_int64, c_int, c_int, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
+                               c_void_p, c_size_t, c_void_p]),
+    "fem_ts_gemm_nn": (c_int, [c_int64, c_int, c_int, c_void_p, c_int64, c_void_p, c_int64, ctypes.c_double,
+                               ctypes.c_double, c_void_p, c_int64, c_void_p]),
     "fem_mlp_backward_tc_workspace_bytes": (c_size_t, [c_int64]),
     "fem_mlp_backward_tc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                     c_size_t, c_void_p, c_void_p]),

@@ -52,8 +52,6 @@ def up_to_date() -> bool:
 def _compile(src: str, extra) -> str:
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
     cmd = [nvcc(), "-c", src, "-o", obj] + NVCC_FLAGS + list(extra)
-    if src.endswith(".cpp"):
-        cmd += ["-x", "cu"] if False else []
     subprocess.run(cmd, check=True)
     return obj
 

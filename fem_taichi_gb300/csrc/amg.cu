@@ -616,12 +616,24 @@ void free_vectors(fem_amg* h) {
     h->vec_nrhs = 0;
 }
 
+void free_dev64(Dev64& D) {
+    cudaFree(D.ptr);
+    cudaFree(D.col);
+    cudaFree(D.val);
+    D = Dev64{};
+}
+
 void free_device(fem_amg* h) {
     free_vectors(h);
     for (Level& L : h->lv) {
         free_bsr(L.dA);
         free_bsr(L.dP);
         free_bsr(L.dR);
+        free_dev64(L.gA);
+        free_dev64(L.gP);
+        free_dev64(L.gR);
+        cudaFree(L.g_dinv);
+        L.g_dinv = nullptr;
         cudaFree(L.d_dinv);
         L.d_dinv = nullptr;
         cudaFree(L.d_iso);
@@ -638,6 +650,8 @@ void free_device(fem_amg* h) {
 }
 
 }  // namespace
+
+void release_device(fem_amg* h) { free_device(h); }
 
 int ensure_vectors(fem_amg* h, int R) {
     if (h->vec_nrhs >= R) return FEM_OK;

@@ -39,6 +39,18 @@ struct DevBsr {
     float* valb = nullptr;  // block-major values
 };
 
+// Device BSR matrix, FP64, block-major values (block l at val[l * br * bc], row-major), 32-bit
+// row pointers: the matrices of a hierarchy set up on the device (amg_device.cu), kept for
+// the next level's setup and for fem_amg_export.
+struct Dev64 {
+    int64_t n = 0, m = 0;
+    int br = 0, bc = 0;
+    int64_t nnzb = 0;
+    int32_t* ptr = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+};
+
 struct Level {
     int b = 0;       // DOF per node
     int64_t n = 0;   // nodes
@@ -59,6 +71,9 @@ struct Level {
     int32_t* d_iso_rows = nullptr;  // indices of the Dirichlet rows (level 0)
     int64_t n_iso = 0;
     float* vfix = nullptr;          // [n_iso][b][nrhs] scratch of the Dirichlet-row update
+    // FP64 device copies of a hierarchy set up on the device (A on levels >= 1)
+    Dev64 gA, gP, gR;
+    double* g_dinv = nullptr;
     // device vectors for the current nrhs ([n][b][nrhs]): right-hand side and output of this
     // level's cycle (levels >= 1), second iterate, Chebyshev direction, residual
     float *vb = nullptr, *vo = nullptr, *vx = nullptr, *vd = nullptr, *vr = nullptr;
@@ -80,6 +95,7 @@ struct fem_amg {
     void* d_state = nullptr;              // solver state used by fem_amg_vcycle (done = 0)
     double setup_s[6] = {0, 0, 0, 0, 0, 0};  // strength+aggregation, tentative, eigen, smoothing, Galerkin, coarse
     bool uploaded = false;
+    bool device_setup = false;            // built by fem_amg_setup_device (FP64 copies on the device)
 };
 
 namespace fem {
@@ -101,6 +117,19 @@ int vcycle(fem_amg* h, const View& A0, const float* r, float* z, const pcgd::Pcg
 
 // Allocates the per-level vectors for nrhs right-hand sides (grow only).
 int ensure_vectors(fem_amg* h, int nrhs);
+
+// Host steps shared by both setups (amg_setup.cpp).
+constexpr int64_t kMaxDense = 8192;   // largest dense coarsest level accepted
+constexpr double kDecoupled2 = 1e-12; // squared scaled coupling below which a row is Dirichlet
+// largest eigenvalue of the symmetric tridiagonal (alpha, beta[1..m-1]) by Sturm bisection
+double tridiag_lmax(const std::vector<double>& alpha, const std::vector<double>& beta);
+// Chebyshev smoother coefficients for `degree` steps on [cheb_upper lmax / cheb_ratio, cheb_upper lmax]
+void chebyshev_coefficients(double lmax, const fem_amg_opts& o, int degree, std::vector<float>& c1,
+                            std::vector<float>& c2);
+// dense inverse with partial pivoting (a is overwritten); false if singular
+bool dense_inverse_host(int64_t m, std::vector<double>& a, std::vector<double>& inv);
+// Releases the device memory of a hierarchy (amg.cu).
+void release_device(fem_amg* h);
 
 }  // namespace amg
 }  // namespace fem

@@ -49,8 +49,6 @@ namespace {
 using Clock = std::chrono::steady_clock;
 double since(Clock::time_point t0) { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
-constexpr int64_t kMaxDense = 8192;  // largest dense coarsest level accepted
-
 // Gauss-Jordan inverse with partial pivoting of a b x b row-major matrix (b <= 6).
 bool invert_small(int b, const double* a, double* inv) {
     double m[kModes][2 * kModes];
@@ -340,8 +338,8 @@ std::vector<uint8_t> strength(const HostBsr& A, const std::vector<double>& G, do
     return s;
 }
 
-// Unaggregated rows whose scaled couplings are all below 1e-6 (squared: 1e-12): Dirichlet.
-constexpr double kDecoupled2 = 1e-12;
+// Unaggregated rows whose scaled couplings are all below 1e-6 (squared: kDecoupled2 = 1e-12)
+// are Dirichlet rows.
 
 int64_t aggregate(const HostBsr& A, const std::vector<uint8_t>& strong, const std::vector<double>& sv,
                   std::vector<int32_t>& agg) {
@@ -804,6 +802,18 @@ int build(fem_amg* H, HostBsr&& A0, const double* xyz) {
 }
 
 }  // namespace
+
+double tridiag_lmax(const std::vector<double>& alpha, const std::vector<double>& beta) {
+    return tridiag_max_eig(alpha, beta);
+}
+void chebyshev_coefficients(double lmax, const fem_amg_opts& o, int degree, std::vector<float>& c1,
+                            std::vector<float>& c2) {
+    chebyshev(lmax, o, degree, c1, c2);
+}
+bool dense_inverse_host(int64_t m, std::vector<double>& a, std::vector<double>& inv) {
+    return dense_inverse(m, a, inv);
+}
+
 }  // namespace amg
 }  // namespace fem
 
@@ -871,6 +881,19 @@ extern "C" int fem_amg_setup(int64_t n_brow, const int32_t* indptr, const int32_
 
 extern "C" int fem_amg_num_levels(const fem_amg* h) { return h ? int(h->lv.size()) : 0; }
 
+extern "C" int fem_amg_set_smoother(fem_amg* h, int level, double upper, double ratio) {
+    FEM_REQUIRE(h, "NULL argument");
+    FEM_REQUIRE(level >= 0 && level + 1 < int(h->lv.size()), "level out of range (the last level is solved densely)");
+    FEM_REQUIRE(upper >= 1.0 && upper <= 4.0 && ratio > 1.0 && ratio <= 1e4,
+                "smoother interval: need 1 <= upper <= 4 and 1 < ratio <= 1e4");
+    Level& L = h->lv[level];
+    fem_amg_opts o = h->opts;
+    o.cheb_upper = upper;
+    o.cheb_ratio = ratio;
+    chebyshev(L.lmax, o, std::max(1, std::max(o.pre_degree, o.post_degree)), L.c1, L.c2);
+    return FEM_OK;
+}
+
 extern "C" int fem_amg_setup_phases(const fem_amg* h, double* seconds6) {
     FEM_REQUIRE(h && seconds6, "NULL argument");
     for (int i = 0; i < 6; ++i) seconds6[i] = h->setup_s[i];
@@ -883,8 +906,8 @@ extern "C" int fem_amg_get_level(const fem_amg* h, int level, fem_amg_level_info
     const Level& L = h->lv[level];
     info->n = L.n;
     info->b = L.b;
-    info->nnzb_A = L.A.nnzb();
-    info->nnzb_P = L.P.nnzb();
+    info->nnzb_A = h->device_setup ? L.gA.nnzb : L.A.nnzb();
+    info->nnzb_P = h->device_setup ? L.gP.nnzb : L.P.nnzb();
     info->lmax = L.lmax;
     info->omega = L.omega;
     info->setup_s = L.setup_s;
@@ -896,6 +919,33 @@ extern "C" int fem_amg_export(const fem_amg* h, int level, int what, int64_t* di
     FEM_REQUIRE(h && dims, "NULL argument");
     FEM_REQUIRE(level >= 0 && level < int(h->lv.size()), "level out of range");
     const Level& L = h->lv[level];
+    if (h->device_setup && (what <= 3)) {  // FP64 copies on the device
+        if (what == 3) {
+            dims[0] = L.n;
+            dims[1] = L.g_dinv ? L.n * L.b * L.b : 0;
+            dims[2] = dims[3] = L.b;
+            if (vals && L.g_dinv)
+                FEM_CUDA(cudaMemcpy(vals, L.g_dinv, sizeof(double) * dims[1], cudaMemcpyDeviceToHost));
+            return FEM_OK;
+        }
+        FEM_REQUIRE(what >= 0, "what must be 0..6");
+        const Dev64& D = what == 0 ? L.gA : what == 1 ? L.gP : L.gR;
+        dims[0] = D.n;
+        dims[1] = D.nnzb;
+        dims[2] = D.br;
+        dims[3] = D.bc;
+        if (D.ptr) {
+            if (indptr) {
+                std::vector<int32_t> p(D.n + 1);
+                FEM_CUDA(cudaMemcpy(p.data(), D.ptr, sizeof(int32_t) * (D.n + 1), cudaMemcpyDeviceToHost));
+                std::copy(p.begin(), p.end(), indptr);
+            }
+            if (indices) FEM_CUDA(cudaMemcpy(indices, D.col, sizeof(int32_t) * D.nnzb, cudaMemcpyDeviceToHost));
+            if (vals)
+                FEM_CUDA(cudaMemcpy(vals, D.val, sizeof(double) * D.nnzb * D.br * D.bc, cudaMemcpyDeviceToHost));
+        }
+        return FEM_OK;
+    }
     const HostBsr* M = nullptr;
     switch (what) {
         case 0: M = &L.A; break;

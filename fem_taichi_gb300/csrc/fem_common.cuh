@@ -42,6 +42,12 @@ inline int cuda_status(cudaError_t e, const char* what) {
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Exclusive scan of cnt[0..n) into out[0..n] (out[n] = total) on stream st (topology_gpu.cu).
+// tiles: device scratch of device_scan_tiles(n) int64 values; bit 1 of *status (device) is
+// set when the total exceeds the int32 range.
+int device_exclusive_scan(int64_t n, const int32_t* cnt, int32_t* out, int64_t* tiles, int* status, cudaStream_t st);
+int64_t device_scan_tiles(int64_t n);
+
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // Gauss abscissa exactly as the reference literal (FEM_model_bsr.py:97).

@@ -281,6 +281,12 @@ int read_status(const int* d_status, cudaStream_t st, int& h) {
 }
 
 }  // namespace
+
+int device_exclusive_scan(int64_t n, const int32_t* cnt, int32_t* out, int64_t* tiles, int* status, cudaStream_t st) {
+    return exclusive_scan(n, cnt, out, tiles, status, st);
+}
+int64_t device_scan_tiles(int64_t n) { return std::max<int64_t>(1, (n + kScanTile - 1) / kScanTile); }
+
 }  // namespace fem
 
 using namespace fem;

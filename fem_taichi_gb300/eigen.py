@@ -10,7 +10,8 @@ Here every vector lives in HBM: M is applied as a BSR SpMM (the scalar-per-block
 expanded to diagonal 3x3 blocks), each K^-1 M u is one multi-right-hand-side PCG solve of the
 whole block (FP32 inner solves inside FP64 refinement, ``fem_pcg_solve`` with the block padded
 to the next supported count; preconditioned by the multigrid V-cycle by default, or block
-Jacobi), and the reorthogonalisation products are FP64 GEMMs on the device.  Only the (2 num_eigen)^2 projection T is diagonalised on the host.
+Jacobi), and the reorthogonalisation products are tall-skinny FP64 kernels on the device
+(fem_ts_gemm_tn / fem_ts_gemm_nn).  Only the (2 num_eigen)^2 projection T is diagonalised on the host.
 
 ``Eigen_solver(Model).Solve_cpu(num_eigen, num_block)`` keeps the reference's signature and
 returns (freq (num_eigen,), vectors (3N, num_eigen)); it runs the GPU path (there is no CPU
@@ -27,6 +28,51 @@ from . import _lib
 from ._lib import FemBsr, FEM_F64
 from .model import _dptr
 from .solve import DeviceSystem, padded_nrhs
+
+
+class _TallSkinny:
+    """FP64 products of a tall block Q (n x m, unit column stride) on the device through
+    fem_ts_gemm_tn / fem_ts_gemm_nn: Q^T X and W = beta W + alpha Q C, split into launches of
+    at most 256 columns of Q and 32 columns of X / W.  The FP64 pipe bounds them; they
+    replace library GEMMs whose tall-skinny shapes ran far below it."""
+
+    def __init__(self, lib, n: int, device, stream):
+        self.lib, self.stream = lib, stream
+        self.ws_bytes = int(lib.fem_ts_gemm_tn_workspace_bytes(n, 256, 32))
+        self.ws = torch.empty(self.ws_bytes // 8 + 1, dtype=torch.float64, device=device)
+
+    @staticmethod
+    def _rows(A: torch.Tensor) -> torch.Tensor:
+        return A if A.stride(1) == 1 else A.contiguous()
+
+    def tn(self, Q: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+        Q, X = self._rows(Q), self._rows(X)
+        n, m = Q.shape
+        b = X.shape[1]
+        C = torch.empty((m, b), dtype=torch.float64, device=Q.device)
+        for j0 in range(0, m, 256):
+            for c0 in range(0, b, 32):
+                _lib.check(self.lib.fem_ts_gemm_tn(n, min(256, m - j0), min(32, b - c0), Q.data_ptr() + 8 * j0,
+                                                   Q.stride(0), X.data_ptr() + 8 * c0, X.stride(0),
+                                                   C.data_ptr() + 8 * (j0 * b + c0), b, _dptr(self.ws),
+                                                   self.ws_bytes, self.stream), "fem_ts_gemm_tn")
+        return C
+
+    def nn(self, Q: torch.Tensor, C: torch.Tensor, W: torch.Tensor, alpha: float, beta: float) -> torch.Tensor:
+        """W = beta W + alpha Q C in place (W must have unit column stride)."""
+        Q, C = self._rows(Q), self._rows(C)
+        if W.stride(1) != 1:
+            raise ValueError("W needs unit column stride")
+        n, m = Q.shape
+        b = C.shape[1]
+        for c0 in range(0, b, 32):
+            for j0 in range(0, m, 256):
+                _lib.check(self.lib.fem_ts_gemm_nn(n, min(256, m - j0), min(32, b - c0), Q.data_ptr() + 8 * j0,
+                                                   Q.stride(0), C.data_ptr() + 8 * (j0 * C.stride(0) + c0),
+                                                   C.stride(0), alpha, beta if j0 == 0 else 1.0,
+                                                   W.data_ptr() + 8 * c0, W.stride(0), self.stream),
+                           "fem_ts_gemm_nn")
+        return W
 
 
 class _PhaseTimes:
@@ -137,28 +183,30 @@ class Eigen_solver:
         u = torch.as_tensor(np.asarray(u0, dtype=np.float64), device=dev).reshape(n, b)
         Q = torch.zeros((n, m), dtype=torch.float64, device=dev)
         T = np.zeros((m, m))
+        ts = _TallSkinny(S.lib, n, dev, S.stream)
         ph = _PhaseTimes(dev)
         with ph.device_phase("m_products"):
             Mu = self._apply_M(u)
         with ph.device_phase("cholesky"):
-            v = torch.linalg.cholesky(u.T @ Mu).T                       # upper, u^T M u = v^T v
+            v = torch.linalg.cholesky(ts.tn(u, Mu)).T                  # upper, u^T M u = v^T v
             u = torch.linalg.solve_triangular(v, u, upper=True, left=False)
         Q[:, :b] = u
         iters = 0
         for i in range(steps):
+            Qs = Q[:, i * b:(i + 1) * b]                                # = u
             with ph.device_phase("m_products"):
-                Mu = self._apply_M(u)
+                Mu = self._apply_M(Qs)
             with ph.device_phase("k_solves"):
                 w, st = S.solve(F=Mu, rtol=rtol, mixed=mixed, precond=pc)
             if st["status"] != 0:
                 raise _lib.FemError(st["status"], f"K solve of Lanczos step {i}: {st['status_text']}")
             iters += st["iterations"]
-            w = w.reshape(n, b)
+            w = w.reshape(n, b).contiguous()
             with ph.device_phase("m_products"):
                 Mw = self._apply_M(w)
             with ph.device_phase("reorth_gemms"):
-                Tii = u.T @ Mw
-                w = w - u @ Tii
+                Tii = ts.tn(Qs, Mw)
+                ts.nn(Qs, Tii, w, -1.0, 1.0)                            # w -= u Tii
             with ph.host_phase("host_copies_eigh"):
                 T[i * b:(i + 1) * b, i * b:(i + 1) * b] = Tii.cpu().numpy()
             if i >= steps - 1:
@@ -168,11 +216,11 @@ class Eigen_solver:
                 with ph.device_phase("m_products"):
                     Mw = self._apply_M(w)
                 with ph.device_phase("reorth_gemms"):
-                    w = w - Qi @ (Qi.T @ Mw)
+                    ts.nn(Qi, ts.tn(Qi, Mw), w, -1.0, 1.0)              # w -= Qi (Qi^T M w)
             with ph.device_phase("m_products"):
                 Mw = self._apply_M(w)
             with ph.device_phase("cholesky"):
-                t = torch.linalg.cholesky(w.T @ Mw).T
+                t = torch.linalg.cholesky(ts.tn(w, Mw)).T
                 u = torch.linalg.solve_triangular(t, w, upper=True, left=False)
             with ph.host_phase("host_copies_eigh"):
                 tn = t.cpu().numpy()
@@ -184,7 +232,8 @@ class Eigen_solver:
         lam = 1.0 / ev
         order = np.argsort(lam)[:num_eigen]
         with ph.device_phase("reorth_gemms"):
-            X = Q @ torch.as_tensor(vec[:, order], device=dev)
+            V = torch.as_tensor(np.ascontiguousarray(vec[:, order]), device=dev)
+            X = ts.nn(Q, V, torch.empty((n, num_eigen), dtype=torch.float64, device=dev), 1.0, 0.0)
         self.last_stats = {"steps": steps, "solve_iterations": iters, "phase_ms": ph.result_ms()}
         return torch.as_tensor(lam[order], device=dev), X
 

@@ -13,6 +13,9 @@ block-scaled operator on the probes.  Forward: ``fem_mlp_forward`` (tcgen05); ba
 ``fem_mlp_backward_tc`` (tcgen05, BF16 operands, FP32 accumulation; ``backward(...,
 tensor_cores=False)`` runs the FP32 CUDA-core kernel ``fem_mlp_backward``); both reduce their
 per-CTA partials in a fixed order (deterministic); optimiser: Adam on FP32 masters.
+
+``LearnedSmoother`` is the second learned form, not block-diagonal: per-level Chebyshev
+smoother weights of the multigrid V-cycle fitted on the same training family.
 """
 from __future__ import annotations
 
@@ -208,3 +211,79 @@ class LearnedPreconditioner:
         _lib.check(self.lib.fem_learned_blocks(data.n, _dptr(out), _dptr(data.ginv), _dptr(P), _stream(self.device)),
                    "fem_learned_blocks")
         return P
+
+
+class LearnedSmoother:
+    """Learned smoother weights of the multigrid V-cycle: a non-block-diagonal learned
+    preconditioner.
+
+    The V-cycle smooths with a Chebyshev polynomial in D^-1 A on [upper lmax / ratio,
+    upper lmax] on every level (``fem_amg_opts``: one (upper, ratio) for all levels).  Here
+    each level index l has its own (upper_l, ratio_l), learned on a family of training systems
+    by minimising the mean log10 of the relative residual that the FP64 multigrid-preconditioned
+    CG reaches after ``iters`` iterations on a seeded random right-hand side (a convergence
+    factor, smooth in the weights).  The search is a coordinate search in log space with
+    shrinking steps over the 2 x ``levels`` weights, started from the default smoother, so
+    the training loss never ends above the default's.  Levels deeper than ``levels`` reuse the
+    last level's weights.  ``apply(hierarchy)`` writes the weights into a hierarchy
+    (``fem_amg_set_smoother``); the preconditioner stays a symmetric V-cycle (the same
+    polynomial before and after the coarse correction), with upper >= 1 so the smoother does
+    not amplify the top of the spectrum.
+    """
+
+    def __init__(self, levels=5, upper=1.1, ratio=30.0):
+        self.upper = [float(upper)] * levels
+        self.ratio = [float(ratio)] * levels
+        self.history = []
+
+    def weights(self, level):
+        k = min(level, len(self.upper) - 1)
+        return self.upper[k], self.ratio[k]
+
+    def apply(self, hierarchy):
+        lib = hierarchy.lib
+        for l in range(int(lib.fem_amg_num_levels(hierarchy.h)) - 1):
+            u, r = self.weights(l)
+            _lib.check(lib.fem_amg_set_smoother(hierarchy.h, l, u, r), "fem_amg_set_smoother")
+        return hierarchy
+
+    def loss(self, cases, iters=12):
+        """Mean log10 relative residual after `iters` FP64 multigrid-PCG iterations over the
+        (system, hierarchy, right-hand side) cases."""
+        tot = 0.0
+        for S, H, F in cases:
+            self.apply(H)
+            _, st = S.solve(F=F, rtol=1e-30, maxit=iters, mixed=False, precond=H, max_outer=1)
+            tot += float(np.log10(max(st["relres"], 1e-300)))
+        return tot / len(cases)
+
+    def fit(self, cases, iters=12, steps=(1.6, 1.25, 1.1), upper_bounds=(1.0, 2.0), ratio_bounds=(3.0, 300.0)):
+        """Coordinate search from the current weights; returns (loss at start, loss at end)."""
+        best = self.loss(cases, iters)
+        start = best
+        self.history = [best]
+        for f in steps:
+            for l in range(len(self.upper)):
+                for name, lo, hi in (("ratio",) + tuple(ratio_bounds), ("upper",) + tuple(upper_bounds)):
+                    vals = getattr(self, name)
+                    cur = vals[l]
+                    for cand in (min(hi, cur * f), max(lo, cur / f)):
+                        if cand == cur:
+                            continue
+                        vals[l] = cand
+                        v = self.loss(cases, iters)
+                        if v < best - 1e-9:
+                            best, cur = v, cand
+                        else:
+                            vals[l] = cur
+                    self.history.append(best)
+        for S, H, F in cases:
+            self.apply(H)
+        return start, best
+
+    def state_dict(self):
+        return {"upper": list(self.upper), "ratio": list(self.ratio)}
+
+    def load_state_dict(self, d):
+        self.upper = [float(x) for x in d["upper"]]
+        self.ratio = [float(x) for x in d["ratio"]]

@@ -46,22 +46,29 @@ def padded_nrhs(r: int) -> int:
 
 
 class AmgHierarchy:
-    """Owner of a ``fem_amg`` hierarchy (host setup + device copy) for one matrix.
+    """Owner of a ``fem_amg`` hierarchy for one matrix.
 
-    Built from the FP64 BSR matrix of a ``DeviceSystem`` (copied to the host for the setup)
-    and the node coordinates (rigid-body modes).  ``opts`` overrides fields of
+    ``AmgHierarchy(lib, n, indptr, indices, vals, xyz, stream)`` sets it up on the host from
+    HOST copies of the FP64 BSR matrix and the node coordinates (``fem_amg_setup``), then
+    uploads it; ``AmgHierarchy.on_device(system)`` sets it up on the device from the
+    system's FP64 matrix (``fem_amg_setup_device``).  ``opts`` overrides fields of
     ``fem_amg_default_opts``."""
 
-    def __init__(self, lib, n, indptr, indices, vals, xyz, stream=None, **opts):
-        import time
-        self.lib = lib
+    @staticmethod
+    def _options(lib, opts):
         o = FemAmgOpts()
         lib.fem_amg_default_opts(ctypes.byref(o))
         for k, v in opts.items():
             if not hasattr(o, k):
                 raise ValueError(f"unknown AMG option {k}")
             setattr(o, k, v)
-        self.opts = o
+        return o
+
+    def __init__(self, lib, n, indptr, indices, vals, xyz, stream=None, **opts):
+        import time
+        self.lib = lib
+        self.where = "host"
+        o = self.opts = self._options(lib, opts)
         ip = np.ascontiguousarray(indptr, dtype=np.int32)
         ix = np.ascontiguousarray(indices, dtype=np.int32)
         va = np.ascontiguousarray(vals, dtype=np.float64)
@@ -76,6 +83,33 @@ class AmgHierarchy:
         if stream is not None:
             _lib.check(lib.fem_amg_upload(self.h, stream), "fem_amg_upload")
         self.upload_s = time.perf_counter() - t0
+
+    @classmethod
+    def on_device(cls, system, **opts):
+        """Set up from ``system.A64`` and the model's device coordinates; the host pattern of
+        the model (``Physics.SmNode`` / ``ReNode``) saves downloading it."""
+        import time
+        self = cls.__new__(cls)
+        self.lib = system.lib
+        self.where = "device"
+        o = self.opts = cls._options(system.lib, opts)
+        xyz = system.model.mesh.xyz.to(torch.float64).contiguous()
+        P = system.model.Physics
+        ip = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+        ix = np.ascontiguousarray(P.ReNode, dtype=np.int32)
+        if ip.shape[0] != system.n + 1 or ix.shape[0] != system.nnzb:
+            ip = ix = None
+        h = ctypes.c_void_p()
+        torch.cuda.synchronize(system.device)
+        t0 = time.perf_counter()
+        _lib.check(system.lib.fem_amg_setup_device(ctypes.byref(system.A64), xyz.data_ptr(),
+                                                   None if ip is None else ip.ctypes.data,
+                                                   None if ix is None else ix.ctypes.data, ctypes.byref(o),
+                                                   system.stream, ctypes.byref(h)), "fem_amg_setup_device")
+        self.h = h
+        self.setup_s = time.perf_counter() - t0
+        self.upload_s = 0.0
+        return self
 
     def levels(self):
         out = []
@@ -185,21 +219,23 @@ class DeviceSystem:
             self._bj = bj
         return self._bj
 
-    def amg(self, **opts) -> AmgHierarchy:
+    def amg(self, setup="device", **opts) -> AmgHierarchy:
         """Smoothed-aggregation multigrid hierarchy of K (built once; ``opts`` as
-        ``fem_amg_opts``).  The setup runs on the host from a copy of K."""
-        if self._amg is None or opts:
-            P = self.model.Physics
-            xyz = self.model.mesh.xyz.cpu().numpy()
-            K = self.K64.reshape(-1).cpu().numpy()
+        ``fem_amg_opts``).  setup: "device" (``fem_amg_setup_device``, from the FP64 matrix in
+        HBM) or "host" (``fem_amg_setup`` on a host copy of K, then uploaded)."""
+        if self._amg is None or opts or self._amg.where != setup:
             if self._amg is not None:
                 self._amg.close()
-            self._amg = AmgHierarchy(self.lib, self.n, P.SmNode, P.ReNode, K, xyz, self.stream, **opts)
+            self._amg = self.amg_variant(setup=setup, **opts)
         return self._amg
 
-    def amg_variant(self, **opts) -> AmgHierarchy:
+    def amg_variant(self, setup="device", **opts) -> AmgHierarchy:
         """A separate multigrid hierarchy of K built with ``opts`` (not cached; pass it to
         ``solve(precond=...)`` and close it when done)."""
+        if setup == "device":
+            return AmgHierarchy.on_device(self, **opts)
+        if setup != "host":
+            raise ValueError("setup must be 'device' or 'host'")
         xyz = self.model.mesh.xyz.cpu().numpy()
         K = self.K64.reshape(-1).cpu().numpy()
         P = self.model.Physics

@@ -25,6 +25,9 @@
  *   fem_bsr_spmv*          SOLVE_static.py:36          KL * U (residual product)
  *   fem_pcg_solve          SOLVE_static.py:31-33       pardisoSolver(KL, mtype=2).factor/solve
  *   fem_amg_*, fem_pcg_solve_amg  SOLVE_static.py:31-33  the same solve, multigrid-preconditioned
+ *                                                      (setup on the host or on the device)
+ *   fem_ts_gemm_*          SOLVE_eigen.py:65-84        Lanczos reorthogonalisation w -= Q (Q^T M w)
+ *                                                      and the Ritz vectors X = Q V (numpy GEMMs)
  */
 #ifndef FEM_GB300_H
 #define FEM_GB300_H
@@ -308,6 +311,18 @@ int fem_pcg_solve(const fem_bsr* A64, const fem_bsr* A32, const double* precond,
                   const fem_pcg_opts* opts, fem_pcg_stats* stats, void* workspace, size_t workspace_bytes,
                   void* stream);
 
+/* ---- tall-skinny FP64 products of the block-Lanczos modal solve -------------------- */
+/* Row-major FP64, DEVICE pointers, 1 <= m <= 256 columns of Q, 1 <= b <= 32.
+ * fem_ts_gemm_tn: C (m x b, leading dimension ldc) = Q^T X for Q n x m (ldq) and X n x b
+ * (ldx); deterministic (per-CTA partials summed in a fixed order).  workspace: at least
+ * fem_ts_gemm_tn_workspace_bytes(n, m, b) bytes of device memory.
+ * fem_ts_gemm_nn: W (n x b, ldw) = beta W + alpha Q C (beta = 0 does not read W). */
+size_t fem_ts_gemm_tn_workspace_bytes(int64_t n, int m, int b);
+int fem_ts_gemm_tn(int64_t n, int m, int b, const double* Q, int64_t ldq, const double* X, int64_t ldx, double* C,
+                   int64_t ldc, void* workspace, size_t workspace_bytes, void* stream);
+int fem_ts_gemm_nn(int64_t n, int m, int b, const double* Q, int64_t ldq, const double* C, int64_t ldc,
+                   double alpha, double beta, double* W, int64_t ldw, void* stream);
+
 /* ---- smoothed-aggregation AMG preconditioner (no reference counterpart) ----------- */
 /* The reference factorises K directly (Pardiso, SOLVE_static.py:31-33).  Block-diagonal
  * preconditioners stall on slender or stretched meshes (condition numbers of 1e9 and more);
@@ -333,6 +348,16 @@ void fem_amg_default_opts(fem_amg_opts* opts);
 int fem_amg_setup(int64_t n_brow, const int32_t* indptr, const int32_t* indices, const double* vals,
                   const double* xyz, const fem_amg_opts* opts, fem_amg** out);
 int fem_amg_upload(fem_amg* amg, void* stream);
+/* The same hierarchy set up on the device: A64 the solver's FP64 matrix (FEM_LAYOUT_BSR,
+ * DEVICE arrays), xyz [n_brow][3] node coordinates (DEVICE).  indptr_host / indices_host: an
+ * optional HOST copy of A64's pattern (NULL: it is downloaded).  Every step runs in FP64
+ * kernels except the two order-dependent greedy passes of the aggregation, which run on the
+ * host from the strong-connection flags (one byte per block).  The result is ready for
+ * fem_pcg_solve_amg (no fem_amg_upload); fem_amg_export reads its FP64 device copies.  Fails
+ * with FEM_ERR_INVALID when a row of a Galerkin product has more than 3072 distinct block
+ * columns (fem_amg_setup has no such limit).  Synchronises the stream. */
+int fem_amg_setup_device(const fem_bsr* A64, const double* xyz, const int32_t* indptr_host,
+                         const int32_t* indices_host, const fem_amg_opts* opts, void* stream, fem_amg** out);
 void fem_amg_destroy(fem_amg* amg);
 typedef struct fem_amg_level_info {
     int64_t n;        /* nodes (block rows) of the level                                    */
@@ -344,6 +369,11 @@ typedef struct fem_amg_level_info {
     double setup_s;   /* host seconds spent building this level's transfer and coarse operator */
 } fem_amg_level_info;
 int fem_amg_num_levels(const fem_amg* amg);
+/* Replaces the Chebyshev smoother of one level (0 <= level < levels - 1) by the polynomial of
+ * the same degree on [upper lmax / ratio, upper lmax] (1 <= upper <= 4, 1 < ratio <= 1e4):
+ * per-level smoother weights, e.g. the learned ones of learned.py:LearnedSmoother.  Takes
+ * effect from the next solve. */
+int fem_amg_set_smoother(fem_amg* amg, int level, double upper, double ratio);
 /* Host seconds of the setup phases summed over the levels: [0] strength + aggregation,
  * [1] tentative prolongator, [2] Lanczos, [3] prolongator smoothing, [4] Galerkin products,
  * [5] dense coarsest inverse. */

@@ -231,3 +231,18 @@ def test_uncoarsenable_large_level_is_refused():
     with pytest.raises(_lib.FemError) as e:
         _setup(Kb, xyz, max_coarse=100)
     assert e.value.code == _lib.FEM_ERR_INVALID
+
+
+def test_set_smoother_checks_its_arguments(built):
+    """fem_amg_set_smoother (per-level smoother weights): accepted on every level but the dense
+    last one, within 1 <= upper <= 4 and 1 < ratio <= 1e4; refused otherwise."""
+    H = built[2]
+    n = len(H.levels())
+    L = H.lib
+    for l in range(n - 1):
+        assert L.fem_amg_set_smoother(H.h, l, 1.2, 20.0) == 0
+    assert L.fem_amg_set_smoother(H.h, n - 1, 1.2, 20.0) == _lib.FEM_ERR_INVALID
+    assert L.fem_amg_set_smoother(H.h, -1, 1.2, 20.0) == _lib.FEM_ERR_INVALID
+    assert L.fem_amg_set_smoother(H.h, 0, 0.9, 20.0) == _lib.FEM_ERR_INVALID
+    assert L.fem_amg_set_smoother(H.h, 0, 1.2, 1.0) == _lib.FEM_ERR_INVALID
+    assert L.fem_amg_set_smoother(H.h, 0, 1.1, 30.0) == 0   # back to the defaults

@@ -61,3 +61,35 @@ def test_fp64_inner_solves_give_the_same_modes():
     b, _ = F.Eigen_solver(M).Solve_gpu(num_eigen=8, num_block=4, u0=u0, mixed=False)
     a, b = a.cpu().numpy(), b.cpu().numpy()
     assert np.all(np.abs(a - b) <= 1e-8 * np.abs(b))
+
+
+@pytest.mark.parametrize("n,m,b", [(1, 1, 1), (1000, 7, 5), (65_559, 200, 10), (40_000, 300, 13), (3_001, 64, 40),
+                                   (129, 256, 32)])
+def test_tall_skinny_products_match_numpy(n, m, b):
+    """fem_ts_gemm_tn / fem_ts_gemm_nn (through the modal solver's wrapper) against numpy FP64
+    on strided column blocks, with the 256-column and 32-column launch splits; the transposed
+    product is deterministic (bitwise equal on a repeat).  Tolerance 1e-13 of |Q|^T |X|."""
+    import torch
+    from fem_taichi_gb300 import _lib
+    from fem_taichi_gb300.eigen import _TallSkinny
+    from fem_taichi_gb300.model import _stream
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(n + m + b)
+    Qf = rng.standard_normal((n, m + 3))
+    X, C, W0 = rng.standard_normal((n, b)), rng.standard_normal((m, b)), rng.standard_normal((n, b + 2))
+    Qd = torch.as_tensor(Qf, device=dev)[:, 2:2 + m]                # leading dimension m + 3
+    ts = _TallSkinny(_lib.load(), n, dev, _stream(dev))
+    Q = Qf[:, 2:2 + m]
+    got = ts.tn(Qd, torch.as_tensor(X, device=dev))
+    again = ts.tn(Qd, torch.as_tensor(X, device=dev))
+    assert torch.equal(got, again)
+    scale = np.abs(Q).T @ np.abs(X)
+    assert np.all(np.abs(got.cpu().numpy() - Q.T @ X) <= 1e-13 * scale)
+    Wd = torch.as_tensor(W0, device=dev)[:, 1:1 + b]
+    ts.nn(Qd, torch.as_tensor(C, device=dev), Wd, -0.5, 2.0)
+    want = 2.0 * W0[:, 1:1 + b] - 0.5 * (Q @ C)
+    scale = 2.0 * np.abs(W0[:, 1:1 + b]) + 0.5 * (np.abs(Q) @ np.abs(C))
+    assert np.all(np.abs(Wd.cpu().numpy() - want) <= 1e-13 * scale)
+    out = torch.full((n, b), np.nan, dtype=torch.float64, device=dev)  # beta = 0 must not read W
+    ts.nn(Qd, torch.as_tensor(C, device=dev), out, 1.0, 0.0)
+    assert np.all(np.abs(out.cpu().numpy() - Q @ C) <= 1e-13 * (np.abs(Q) @ np.abs(C)))
