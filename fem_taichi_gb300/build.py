@@ -49,9 +49,17 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(p) <= t for p in _deps() + [__file__])
 
 
+# The two multigrid setups must round alike (the device hierarchy is bit-identical to the host
+# one): no contraction of a multiply and an add into an FMA in either translation unit.
+PER_FILE_FLAGS = {
+    "amg_device.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "amg_setup.cpp": ["-Xcompiler", "-ffp-contract=off"],
+}
+
+
 def _compile(src: str, extra) -> str:
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
-    cmd = [nvcc(), "-c", src, "-o", obj] + NVCC_FLAGS + list(extra)
+    cmd = [nvcc(), "-c", src, "-o", obj] + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + list(extra)
     subprocess.run(cmd, check=True)
     return obj
 

@@ -120,6 +120,10 @@ int ensure_vectors(fem_amg* h, int nrhs);
 
 // Host steps shared by both setups (amg_setup.cpp).
 constexpr int64_t kMaxDense = 8192;   // largest dense coarsest level accepted
+// Sums over long vectors (Lanczos dot products, the centroid of the node coordinates) are
+// taken in chunks of kSumChunk consecutive elements, each summed in order, and the chunk
+// sums added in order: the same sequence of roundings on the host and on the device.
+constexpr int64_t kSumChunk = 2048;
 constexpr double kDecoupled2 = 1e-12; // squared scaled coupling below which a row is Dirichlet
 // largest eigenvalue of the symmetric tridiagonal (alpha, beta[1..m-1]) by Sturm bisection
 double tridiag_lmax(const std::vector<double>& alpha, const std::vector<double>& beta);

@@ -10,13 +10,19 @@
 // the node order); they read the strong-connection flags (one byte per block).  Step (b)
 // (join the most strongly coupled aggregate) is independent per node and runs on the device.
 //
-// Kernels (FP64, deterministic: every sum has a fixed order):
+// The hierarchy is bit-identical to the host setup's: every value is produced by the same
+// sequence of IEEE operations on both sides (this file is compiled with -fmad=false and the
+// host setup with -ffp-contract=off, so neither fuses a multiply and an add on its own; the
+// sparse products use explicit fma() on both sides), and every sum runs in the host's order
+// -- per-row loops in the same order, long sums in kSumChunk chunks.
+//
+// Kernels (FP64):
 //  k_diag        per row: diagonal position, Gauss-Jordan inverse of the diagonal block,
 //                inverse Cholesky factor L_i^-1 (the strength scaling)
 //  k_strength    per block: |L_i^-1 A_ij L_j^-T|_F^2, strong flag
-//  k_tentative   one warp per aggregate: two-pass modified Gram-Schmidt of the aggregate's
+//  k_tentative   one thread per aggregate: two-pass modified Gram-Schmidt of the aggregate's
 //                rows of the near-null space (columns dropped when dependent)
-//  k_spmv64 ...  Lanczos: block-row product, block-diagonal products, fixed-grid dot products
+//  k_spmv64 ...  Lanczos: block-row product, block-diagonal products, chunked dot products
 //  k_prol_*      one warp per row: the distinct aggregates of the row's neighbours (sorted),
 //                then P_ia = -omega D_i^-1 sum_j A_ij T_j (+ T_i on the row's own aggregate)
 //  k_tr_*        R = P^T: column counts, scan, scatter, then a per-row sort by fine row
@@ -43,7 +49,6 @@ double since(Clock::time_point t0) { return std::chrono::duration<double>(Clock:
 constexpr int kT = 256;
 constexpr int kWarps = kT / 32;
 constexpr int kHashCap = 4096;     // distinct columns of one Galerkin row: at most 3/4 of this
-constexpr int kDotBlocks = 256;    // fixed grid of the deterministic reductions
 constexpr int32_t kFree = -1, kAlone = -2;
 
 unsigned grid(int64_t work, int threads) {
@@ -279,62 +284,49 @@ __global__ void k_rigid_modes(int64_t n, const double* __restrict__ xyz, double 
     }
 }
 
-// sum over the warp, the same value in every lane
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return __shfl_sync(0xffffffffu, v, 0);
-}
-
-// One warp per aggregate: T rows of the members (T[node][B][6], rows in member order) =
-// the aggregate's rows of the near-null space, orthonormalised column by column; Bc[a] = R.
+// One thread per aggregate, in the host setup's order (amg_setup.cpp:tentative): T rows of
+// the members (T[node][B][6], rows in member order) = the aggregate's rows of the near-null
+// space, orthonormalised column by column by two-pass modified Gram-Schmidt; Bc[a] = R.
 template <int B>
 __global__ void k_tentative(int64_t na, const int32_t* __restrict__ aptr, const int32_t* __restrict__ mem,
                             const double* __restrict__ Bn, double* T, double* Bc) {
     constexpr int k = kModes;
-    const int lane = threadIdx.x & 31;
-    const int64_t a = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (a >= na) return;
-    const int s0 = aptr[a], cnt = aptr[a + 1] - s0, rows = cnt * B;
-    auto rowp = [&](int r) { return T + (int64_t(mem[s0 + r / B]) * B + r % B) * k; };
-    for (int r = lane; r < rows; r += 32) {
-        const double* src = Bn + (int64_t(mem[s0 + r / B]) * B + r % B) * k;
-        double* dst = rowp(r);
-        for (int m = 0; m < k; ++m) dst[m] = src[m];
-    }
-    __syncwarp();
-    double R[k][k];
-    for (int i = 0; i < k; ++i)
-        for (int j = 0; j < k; ++j) R[i][j] = 0.0;
-    for (int c = 0; c < k; ++c) {
-        double s = 0.0;
-        for (int r = lane; r < rows; r += 32) {
-            const double q = rowp(r)[c];
-            s += q * q;
+    for (int64_t a = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; a < na; a += int64_t(gridDim.x) * blockDim.x) {
+        const int s0 = aptr[a], cnt = aptr[a + 1] - s0, rows = cnt * B;
+        auto rowp = [&](int r) { return T + (int64_t(mem[s0 + r / B]) * B + r % B) * k; };
+        for (int r = 0; r < rows; ++r) {
+            const double* src = Bn + (int64_t(mem[s0 + r / B]) * B + r % B) * k;
+            double* dst = rowp(r);
+            for (int m = 0; m < k; ++m) dst[m] = src[m];
         }
-        const double n0 = sqrt(warp_sum(s));
-        for (int pass = 0; pass < 2; ++pass)
-            for (int c2 = 0; c2 < c; ++c2) {
-                double d = 0.0;
-                for (int r = lane; r < rows; r += 32) d += rowp(r)[c2] * rowp(r)[c];
-                d = warp_sum(d);
-                for (int r = lane; r < rows; r += 32) rowp(r)[c] -= d * rowp(r)[c2];
-                R[c2][c] += d;
+        double R[k][k];
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) R[i][j] = 0.0;
+        for (int c = 0; c < k; ++c) {
+            double n0 = 0.0;
+            for (int r = 0; r < rows; ++r) n0 += rowp(r)[c] * rowp(r)[c];
+            n0 = sqrt(n0);
+            for (int pass = 0; pass < 2; ++pass)
+                for (int c2 = 0; c2 < c; ++c2) {
+                    double d = 0.0;
+                    for (int r = 0; r < rows; ++r) d += rowp(r)[c2] * rowp(r)[c];
+                    for (int r = 0; r < rows; ++r) rowp(r)[c] -= d * rowp(r)[c2];
+                    R[c2][c] += d;
+                }
+            double nr = 0.0;
+            for (int r = 0; r < rows; ++r) nr += rowp(r)[c] * rowp(r)[c];
+            nr = sqrt(nr);
+            if (nr > 1e-10 * n0 && nr > 0.0) {
+                for (int r = 0; r < rows; ++r) rowp(r)[c] /= nr;
+                R[c][c] = nr;
+            } else {
+                for (int r = 0; r < rows; ++r) rowp(r)[c] = 0.0;
+                R[c][c] = 0.0;
             }
-        s = 0.0;
-        for (int r = lane; r < rows; r += 32) {
-            const double q = rowp(r)[c];
-            s += q * q;
         }
-        const double nr = sqrt(warp_sum(s));
-        const bool keep = nr > 1e-10 * n0 && nr > 0.0;
-        for (int r = lane; r < rows; r += 32) rowp(r)[c] = keep ? rowp(r)[c] / nr : 0.0;
-        R[c][c] = keep ? nr : 0.0;
-        __syncwarp();
-    }
-    if (lane == 0)
         for (int i = 0; i < k; ++i)
             for (int j = 0; j < k; ++j) Bc[(a * k + i) * k + j] = R[i][j];
+    }
 }
 
 // ---- Lanczos estimate of lambda_max(D^-1 A) ---------------------------------------------------
@@ -378,21 +370,21 @@ __global__ void k_splitmix(int64_t N, double* v) {
     }
 }
 
-// part[block] = sum of a[i] * b[i] (b == nullptr: a[i * stride + off]) over the block's
-// grid-stride elements; fixed grid, so the host's ordered sum of the parts is deterministic
-__global__ void __launch_bounds__(kT) k_dot_part(int64_t N, const double* __restrict__ a, const double* __restrict__ b,
-                                                 int stride, int off, double* part) {
-    __shared__ double sh[kT];
-    double s = 0.0;
-    for (int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x; i < N; i += int64_t(kDotBlocks) * kT)
-        s += b ? a[i] * b[i] : a[i * stride + off];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = kT / 2; w > 0; w >>= 1) {
-        if (int(threadIdx.x) < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-        __syncthreads();
+// part[c] = sum over chunk c (kSumChunk consecutive elements, in order) of a[i] * b[i], or of
+// a[i * stride + off] when b is null: the host setup's order (amg_setup.cpp:dot)
+__global__ void k_chunk_sums(int64_t N, const double* __restrict__ a, const double* __restrict__ b, int stride,
+                             int off, double* part) {
+    const int64_t nc = (N + kSumChunk - 1) / kSumChunk;
+    for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < nc; c += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t e = std::min(N, (c + 1) * kSumChunk);
+        double s = 0.0;
+        if (b) {
+            for (int64_t i = c * kSumChunk; i < e; ++i) s += a[i] * b[i];
+        } else {
+            for (int64_t i = c * kSumChunk; i < e; ++i) s += a[i * stride + off];
+        }
+        part[c] = s;
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
 __global__ void k_lanczos_w(int64_t N, double* w, double a, const double* __restrict__ v, double bj,
@@ -452,19 +444,30 @@ __global__ void k_prol_count(int64_t n, const int32_t* __restrict__ ptr, const i
     }
 }
 
+// Per row: the sorted distinct aggregates u of the row's neighbours (rank order), then for
+// every (u, entry (r, c)) -- lanes over these items, so all lanes do FP64 work --
+// acc = sum over the row's entries l with aggregate u, ascending, of sum_q A_il[r][q] T_l[q][c]
+// (the host's Gustavson order), and P_iu = -omega D_i^-1 acc (+ T_i on the row's own
+// aggregate).  Shared memory per warp: keys and first-occurrence flags (maxL each), the
+// distinct keys (maxU) and the accumulators (maxU blocks).
 template <int B>
 __global__ void k_prol_fill(int64_t n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                             const double* __restrict__ val, const int32_t* __restrict__ agg,
                             const uint8_t* __restrict__ iso, int smooth, double omega, const double* __restrict__ dinv,
-                            const double* __restrict__ T, int maxL, const int32_t* __restrict__ pptr, int32_t* pcol,
-                            double* pval) {
+                            const double* __restrict__ T, int maxL, int maxU, int warps,
+                            const int32_t* __restrict__ pptr, int32_t* pcol, double* pval) {
     constexpr int k = kModes, BK = B * k;
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int32_t* keys = reinterpret_cast<int32_t*>(smem) + w * maxL;
-    uint8_t* flags = reinterpret_cast<uint8_t*>(reinterpret_cast<int32_t*>(smem) + kWarps * maxL) + w * maxL;
-    const int64_t nw = int64_t(gridDim.x) * kWarps;
-    for (int64_t i = int64_t(blockIdx.x) * kWarps + w; i < n; i += nw) {
+    const size_t per = size_t(maxU) * BK * sizeof(double) + size_t(maxL + maxU) * sizeof(int32_t) + maxL;
+    const size_t per_al = (per + 15) & ~size_t(15);
+    unsigned char* base = smem + w * per_al;
+    double* acc = reinterpret_cast<double*>(base);
+    int32_t* keys = reinterpret_cast<int32_t*>(acc + size_t(maxU) * BK);
+    int32_t* ukeys = keys + maxL;
+    uint8_t* flags = reinterpret_cast<uint8_t*>(ukeys + maxU);
+    const int64_t nw = int64_t(gridDim.x) * warps;
+    for (int64_t i = int64_t(blockIdx.x) * warps + w; i < n; i += nw) {
         if (!smooth) {
             if (lane == 0 && agg[i] >= 0) {
                 const int p = pptr[i];
@@ -475,38 +478,36 @@ __global__ void k_prol_fill(int64_t n, const int32_t* __restrict__ ptr, const in
         }
         if (iso[i]) continue;
         const int rs = ptr[i], L = ptr[i + 1] - rs;
+        const int ps = pptr[i], U = pptr[i + 1] - ps;
         for (int q = lane; q < L; q += 32) keys[q] = agg[col[rs + q]];
         __syncwarp();
         mark_first(keys, L, flags, lane);
-        const double* di = dinv + i * B * B;
-        const int32_t own = agg[i];
-        for (int q = lane; q < L; q += 32) {
-            if (!flags[q]) continue;
-            const int32_t kc = keys[q];
-            const int out = pptr[i] + rank_of(keys, flags, L, kc);
-            double acc[B][k];
-            for (int r = 0; r < B; ++r)
-                for (int c = 0; c < k; ++c) acc[r][c] = 0.0;
+        for (int q = lane; q < L; q += 32)
+            if (flags[q]) ukeys[rank_of(keys, flags, L, keys[q])] = keys[q];
+        __syncwarp();
+        for (int it = lane; it < U * BK; it += 32) {
+            const int u = it / BK, e = it - u * BK, r = e / k, c = e - r * k;
+            const int32_t kc = ukeys[u];
+            double a = 0.0;
             for (int l = 0; l < L; ++l) {
                 if (keys[l] != kc) continue;
-                const double* a = val + int64_t(rs + l) * B * B;
-                const double* t = T + int64_t(col[rs + l]) * BK;
-                for (int r = 0; r < B; ++r)
-                    for (int qq = 0; qq < B; ++qq) {
-                        const double av = a[r * B + qq];
-                        for (int c = 0; c < k; ++c) acc[r][c] += av * t[qq * k + c];
-                    }
+                const double* ab = val + int64_t(rs + l) * B * B + r * B;
+                const double* t = T + int64_t(col[rs + l]) * BK + c;
+                for (int q = 0; q < B; ++q) a = fma(ab[q], t[q * k], a);
             }
-            double* o = pval + int64_t(out) * BK;
-            for (int r = 0; r < B; ++r)
-                for (int c = 0; c < k; ++c) {
-                    double s = 0.0;
-                    for (int qq = 0; qq < B; ++qq) s += di[r * B + qq] * acc[qq][c];
-                    double v = -omega * s;
-                    if (kc == own) v += T[i * BK + r * k + c];
-                    o[r * k + c] = v;
-                }
-            pcol[out] = kc;
+            acc[it] = a;
+        }
+        __syncwarp();
+        const double* di = dinv + i * B * B;
+        const int32_t own = agg[i];
+        for (int it = lane; it < U * BK; it += 32) {
+            const int u = it / BK, e = it - u * BK, r = e / k, c = e - r * k;
+            double sdot = 0.0;
+            for (int q = 0; q < B; ++q) sdot += di[r * B + q] * acc[u * BK + q * k + c];
+            double v = -omega * sdot;
+            if (ukeys[u] == own) v += T[i * BK + e];
+            pval[int64_t(ps + u) * BK + e] = v;
+            if (e == 0) pcol[ps + u] = ukeys[u];
         }
         __syncwarp();
     }
@@ -711,7 +712,7 @@ __global__ void k_sg_fill(int64_t n, const int32_t* __restrict__ xptr, const int
                     double* z = zval + (int64_t(zs) + pb[t]) * ZB + e;
                     double acc = *z;
 #pragma unroll
-                    for (int q = 0; q < BK; ++q) acc += xb[r * BK + q] * yb[q * BJ + c];
+                    for (int q = 0; q < BK; ++q) acc = fma(xb[r * BK + q], yb[q * BJ + c], acc);
                     *z = acc;
                 }
                 __syncwarp();
@@ -761,6 +762,7 @@ struct Setup {
     fem_amg* H;
     cudaStream_t st;
     DBuf parts, status, tiles;
+    size_t parts_n = 0;
 
     int sync() { return cuda_status(cudaStreamSynchronize(st), "cudaStreamSynchronize (AMG setup)"); }
     template <typename T>
@@ -774,12 +776,18 @@ struct Setup {
         if (!h.empty()) FEM_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
         return sync();  // h may be freed by the caller
     }
-    // deterministic sum over N: a[i] * b[i], or a[i * stride + off] when b is null
+    // sum over N of a[i] * b[i], or of a[i * stride + off] when b is null, in the host
+    // setup's order: chunk sums on the device, added in chunk order here
     int dot(int64_t N, const double* a, const double* b, double& out, int stride = 1, int off = 0) {
-        k_dot_part<<<kDotBlocks, kT, 0, st>>>(N, a, b, stride, off, parts.as<double>());
-        FEM_LAUNCH_CHECK("k_dot_part");
+        const int64_t nc = (N + kSumChunk - 1) / kSumChunk;
+        if (int64_t(parts_n) < nc) {
+            FEM_TRY(parts.alloc(sizeof(double) * nc));
+            parts_n = size_t(nc);
+        }
+        k_chunk_sums<<<grid(nc, 64), 64, 0, st>>>(N, a, b, stride, off, parts.as<double>());
+        FEM_LAUNCH_CHECK("k_chunk_sums");
         std::vector<double> h;
-        FEM_TRY(down(h, parts.as<const double>(), kDotBlocks));
+        FEM_TRY(down(h, parts.as<const double>(), size_t(nc)));
         double s = 0.0;
         for (double v : h) s += v;
         out = s;
@@ -1159,8 +1167,8 @@ int level_kernels(Setup& S, fem_amg* H, int l, const View& A, const double* Bnul
     FEM_TRY(Bnext.alloc(sizeof(double) * na * kModes * kModes));
     FEM_TRY(S.up(daptr.as<int32_t>(), aptr));
     FEM_TRY(S.up(dmem.as<int32_t>(), mem));
-    k_tentative<B><<<grid(na * 32, kT), kT, 0, S.st>>>(na, daptr.as<int32_t>(), dmem.as<int32_t>(), Bnull_in,
-                                                       T.as<double>(), Bnext.as<double>());
+    k_tentative<B><<<grid(na, 64), 64, 0, S.st>>>(na, daptr.as<int32_t>(), dmem.as<int32_t>(), Bnull_in,
+                                                   T.as<double>(), Bnext.as<double>());
     FEM_LAUNCH_CHECK("k_tentative");
     FEM_TRY(S.sync());
     H->setup_s[1] += since(tt);
@@ -1190,11 +1198,19 @@ int level_kernels(Setup& S, fem_amg* H, int l, const View& A, const double* Bnul
         P.nnzb = nnz;
         FEM_TRY(P.col.alloc(sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
         FEM_TRY(P.val.alloc(sizeof(double) * std::max<int64_t>(nnz, 1) * B * kModes));
-        FEM_CUDA(cudaFuncSetAttribute(k_prol_fill<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        k_prol_fill<B><<<grid(n, kWarps), kT, smem, S.st>>>(n, A.ptr, A.col, A.val, agg.as<int32_t>(),
-                                                            iso.as<uint8_t>(), o.smooth != 0, L.omega,
-                                                            dinv64.as<double>(), T.as<double>(), maxL, P.P(),
-                                                            P.col.as<int32_t>(), P.val.as<double>());
+        int maxU = 1;
+        FEM_TRY(max_row_len(S, View{n, na, B, kModes, nnz, P.P(), nullptr, nullptr}, maxU));
+        maxU = std::max(maxU, 1);
+        const size_t per = size_t(maxU) * B * kModes * sizeof(double) + size_t(maxL + maxU) * sizeof(int32_t) + maxL;
+        const size_t per_al = (per + 15) & ~size_t(15);
+        int warps = kWarps;
+        while (warps > 1 && per_al * warps > 200 * 1024) warps >>= 1;
+        FEM_REQUIRE(per_al * warps <= 220 * 1024, "AMG device setup: level %d needs %zu bytes per prolongator row", l,
+                    per_al);
+        FEM_CUDA(cudaFuncSetAttribute(k_prol_fill<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per_al * warps)));
+        k_prol_fill<B><<<grid(n, warps), 32 * warps, per_al * warps, S.st>>>(
+            n, A.ptr, A.col, A.val, agg.as<int32_t>(), iso.as<uint8_t>(), o.smooth != 0, L.omega, dinv64.as<double>(),
+            T.as<double>(), maxL, maxU, warps, P.P(), P.col.as<int32_t>(), P.val.as<double>());
         FEM_LAUNCH_CHECK("k_prol_fill");
         FEM_TRY(S.sync());
     }
@@ -1224,14 +1240,13 @@ int level_kernels(Setup& S, fem_amg* H, int l, const View& A, const double* Bnul
 int build_device(fem_amg* H, const fem_bsr* A64, const double* xyz, const int32_t* hptr, const int32_t* hcol,
                  cudaStream_t st) {
     Setup S{H, st};
-    FEM_TRY(S.parts.alloc(sizeof(double) * kDotBlocks));
     FEM_TRY(S.status.alloc(sizeof(int)));
     const int64_t n0 = A64->n_brow;
     // level-0 near-null space: rigid-body modes about the centroid
     DBuf Bnull;
     FEM_TRY(Bnull.alloc(sizeof(double) * n0 * 3 * kModes));
     {
-        double c[3];
+        double c[3];  // the host setup's chunked centroid
         for (int d = 0; d < 3; ++d) {
             FEM_TRY(S.dot(n0, xyz, nullptr, c[d], 3, d));
             c[d] /= double(n0);

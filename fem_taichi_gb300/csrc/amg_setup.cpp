@@ -37,6 +37,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <new>
 #include <vector>
 
@@ -161,7 +162,7 @@ void block_apply(int64_t n, int b, const double* M, const double* x, double* y) 
 double dot(const std::vector<double>& a, const std::vector<double>& b) {
     // fixed-shape reduction: per-chunk partial sums added in chunk order
     const int64_t n = int64_t(a.size());
-    const int64_t chunk = 1 << 16;
+    const int64_t chunk = kSumChunk;
     const int64_t nc = (n + chunk - 1) / chunk;
     std::vector<double> part(std::max<int64_t>(nc, 1), 0.0);
 #pragma omp parallel for schedule(static)
@@ -457,13 +458,14 @@ void tentative(int64_t n, int b, const std::vector<int32_t>& agg, int64_t na, co
     }
 }
 
-// z (BI x BJ) += x (BI x BK) y (BK x BJ); block shapes fixed at compile time
+// z (BI x BJ) += x (BI x BK) y (BK x BJ); block shapes fixed at compile time.  Every term is
+// one correctly rounded fused multiply-add, as in the device setup's products.
 template <int BI, int BK, int BJ>
 inline void block_fma(const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ z) {
     for (int r = 0; r < BI; ++r)
         for (int q = 0; q < BK; ++q) {
             const double xv = x[r * BK + q];
-            for (int c = 0; c < BJ; ++c) z[r * BJ + c] += xv * y[q * BJ + c];
+            for (int c = 0; c < BJ; ++c) z[r * BJ + c] = std::fma(xv, y[q * BJ + c], z[r * BJ + c]);
         }
 }
 
@@ -691,9 +693,14 @@ int build(fem_amg* H, HostBsr&& A0, const double* xyz) {
     {
         const int64_t n = A.n;
         double c[3] = {0, 0, 0};
-        for (int64_t i = 0; i < n; ++i)
-            for (int d = 0; d < 3; ++d) c[d] += xyz[3 * i + d];
-        for (int d = 0; d < 3; ++d) c[d] /= double(n);
+        for (int d = 0; d < 3; ++d) {  // chunked like dot()
+            for (int64_t c0 = 0; c0 < n; c0 += kSumChunk) {
+                double s = 0.0;
+                for (int64_t i = c0; i < std::min(n, c0 + kSumChunk); ++i) s += xyz[3 * i + d];
+                c[d] += s;
+            }
+            c[d] /= double(n);
+        }
         B.assign(size_t(n) * 3 * kModes, 0.0);
         for (int64_t i = 0; i < n; ++i) {
             const double x = xyz[3 * i] - c[0], y = xyz[3 * i + 1] - c[1], z = xyz[3 * i + 2] - c[2];

@@ -371,8 +371,10 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams p) {
 // lane-per-slot path (same order).
 constexpr int kG64Warps = 4;
 constexpr int kG64Rows = 4;
-constexpr int kG64MaxL = 32;
-constexpr int kG64RowStride = kG64MaxL * kPairStride + 4;  // +4 doubles: rows start 8 banks apart
+// 27 slots: every row of a structured hex mesh (3 x 3 x 3 neighbour nodes); the row
+// accumulators of a CTA then take 37 KB, so 6 CTAs (24 warps) fit on an SM instead of 5.
+constexpr int kG64MaxL = 27;
+constexpr int kG64RowStride = kG64MaxL * kPairStride + 6;  // +6 doubles: rows start 8 banks apart
 
 struct Gather64Params {
     int64_t row_begin, row_end;  // block rows [row_begin, row_end) of this launch

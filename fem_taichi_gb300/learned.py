@@ -219,7 +219,9 @@ class LearnedSmoother:
 
     The V-cycle smooths with a Chebyshev polynomial in D^-1 A on [upper lmax / ratio,
     upper lmax] on every level (``fem_amg_opts``: one (upper, ratio) for all levels).  Here
-    each level index l has its own (upper_l, ratio_l), learned on a family of training systems
+    the first ``levels`` level indices have their own (upper_l, ratio_l) (the default, 2:
+    the fine level and one pair shared by every coarser level, which keeps the weights from
+    fitting the depth of the training hierarchies), learned on a family of training systems
     by minimising the mean log10 of the relative residual that the FP64 multigrid-preconditioned
     CG reaches after ``iters`` iterations on a seeded random right-hand side (a convergence
     factor, smooth in the weights).  The search is a coordinate search in log space with
@@ -231,7 +233,7 @@ class LearnedSmoother:
     not amplify the top of the spectrum.
     """
 
-    def __init__(self, levels=5, upper=1.1, ratio=30.0):
+    def __init__(self, levels=2, upper=1.1, ratio=30.0):
         self.upper = [float(upper)] * levels
         self.ratio = [float(ratio)] * levels
         self.history = []
@@ -257,7 +259,7 @@ class LearnedSmoother:
             tot += float(np.log10(max(st["relres"], 1e-300)))
         return tot / len(cases)
 
-    def fit(self, cases, iters=12, steps=(1.6, 1.25, 1.1), upper_bounds=(1.0, 2.0), ratio_bounds=(3.0, 300.0)):
+    def fit(self, cases, iters=12, steps=(1.6, 1.25, 1.1), upper_bounds=(1.0, 1.6), ratio_bounds=(6.0, 120.0)):
         """Coordinate search from the current weights; returns (loss at start, loss at end)."""
         best = self.loss(cases, iters)
         start = best

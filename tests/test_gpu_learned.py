@@ -179,13 +179,15 @@ def _timed_rows(S, Fm, Ur, variants):
     rows = {}
     for label, kw in variants:
         S.solve(F=Fm, rtol=1e-10, **kw)                      # warm: graphs, autotune, FP32 copy
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        U, st = S.solve(F=Fm, rtol=1e-10, **kw)
-        torch.cuda.synchronize()
+        wall = None
+        for _ in range(2):                                    # best of two timed solves
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            U, st = S.solve(F=Fm, rtol=1e-10, **kw)
+            torch.cuda.synchronize()
+            wall = min(wall or 1e30, time.perf_counter() - t)
         err = float(((U - Ur).norm(dim=0) / Ur.norm(dim=0)).max())
-        rows[label] = dict(wall=time.perf_counter() - t, it=st["iterations"], outer=st["outer"], status=st["status"],
-                           err=err)
+        rows[label] = dict(wall=wall, it=st["iterations"], outer=st["outer"], status=st["status"], err=err)
     return rows
 
 
@@ -227,13 +229,14 @@ def test_learned_preconditioner_gain_on_a_held_out_mesh(capsys):
 
 def test_learned_smoother_gain_on_a_held_out_mesh(capsys):
     """The non-block-diagonal learned form: per-level Chebyshev smoother weights of the
-    multigrid V-cycle, learned on 6 blocks of the c4 family (learned.py:LearnedSmoother).
+    multigrid V-cycle (fine level, and one pair for the coarser levels), learned on 6 blocks of
+    the c4 family (learned.py:LearnedSmoother).
     Prints, on the held-out block, the FP64 multigrid solve's iterations and wall time with the
     learned weights over the default smoother, for 1 and 32 right-hand sides.  Asserted: the
     training loss does not end above the default's, every solve reaches 1e-8 against the FP64
     reference, and the learned weights cost at most 1.1x the default's iterations."""
     import bench_solve
-    sm, info = bench_solve.train_smoother(count=6, seed=3, min_nodes=8_000, max_nodes=40_000)
+    sm, info = bench_solve.train_smoother(count=6, seed=3, min_nodes=20_000, max_nodes=100_000)
     assert info["loss_end"] <= info["loss_start"]
     S = _held_out_system()
     Hd, Hl = S.amg_variant(), sm.apply(S.amg_variant())
