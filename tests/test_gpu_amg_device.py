@@ -71,3 +71,57 @@ def test_device_hierarchy_solves_like_the_host_hierarchy(pair):
         U = U.cpu().numpy().reshape(-1)
         assert np.linalg.norm(U - Ur) <= 1e-8 * np.linalg.norm(Ur), name
     assert its["device"] == its["host"], its
+
+
+def _exports(H):
+    out = []
+    info = H.levels()
+    for l, inf in enumerate(info):
+        out.append(("lmax", l, inf["lmax"], inf["n"], inf["b"], inf["nnzb_A"], inf["nnzb_P"]))
+        out.append(("dinv", l, H.export(l, 3)))
+        if l > 0:
+            out.append(("A", l) + tuple(H.export(l, 0)))
+        if l + 1 < len(info):
+            out += [("agg", l, H.export(l, 4)), ("iso", l, H.export(l, 6))]
+            out += [("P", l) + tuple(H.export(l, 1)), ("R", l) + tuple(H.export(l, 2))]
+    out.append(("coarse", H.export(len(info) - 1, 5)))
+    return out
+
+
+def _same(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert len(x) == len(y) and x[0] == y[0], (x[0], y[0])
+        for u, v in zip(x[1:], y[1:]):
+            if isinstance(u, np.ndarray):
+                assert np.array_equal(u, v), x[:2]
+            else:
+                assert u == v, x[:2]
+
+
+@pytest.mark.parametrize("case", ["unsmoothed", "single_dense_level", "all_penalised", "theta0_two_levels"])
+def test_device_setup_edge_cases_bit_identical(case):
+    """Options and shapes off the main path, device vs host setup, every array exactly equal:
+    P = T (smooth = 0), a system small enough to be one dense level, a mesh whose every node
+    is penalised (no aggregate: one dense level), and theta = 0 with a two-level cap."""
+    if case == "all_penalised":
+        from fem_taichi_gb300.mesh import block_arrays
+        b = block_arrays(3, 3, 2, jitter=0.1, seed=2, fix=None)
+        P = F.Physics(b["ids"], b["xyz"], b["elem"], [[np.arange(b["xyz"].shape[0]), [0, 0, 0]]], [], name="fixed")
+    else:
+        P = F.hex_block(10, 8, 6, jitter=0.1, seed=7, fix="zmin", load_face="zmax", load=(0, 0, -1.0))
+    opts = {"unsmoothed": dict(smooth=0, max_coarse=60), "single_dense_level": dict(max_coarse=100000),
+            "all_penalised": dict(max_coarse=10), "theta0_two_levels": dict(theta=0.0, max_levels=2,
+                                                                           max_coarse=10)}[case]
+    S = F.DeviceSystem(F.Model(case, P, STEEL))
+    Hd = S.amg_variant(setup="device", **opts)
+    Hh = S.amg_variant(setup="host", **opts)
+    try:
+        if case in ("single_dense_level", "all_penalised"):
+            assert len(Hd.levels()) == 1
+        else:
+            assert len(Hd.levels()) >= 2
+        _same(_exports(Hd), _exports(Hh))
+    finally:
+        Hd.close()
+        Hh.close()
