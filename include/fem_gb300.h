@@ -158,7 +158,8 @@ int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const
  * overlap the kernels.  The plan comes from fem_pipeline_plan.  Host buffers may be
  * page-locked (copies asynchronous) or pageable (copies then finish before the call
  * returns).  `stream` is ordered after the last copy: synchronise it before reading the host
- * buffers.  Not capturable into a CUDA graph.  FEM_ALGO_FP64 runs as a single part. */
+ * buffers.  Not capturable into a CUDA graph.  FEM_ALGO_FP64 without mesh->slot_map runs as
+ * a single part. */
 int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
                       const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
                       int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
