@@ -361,6 +361,7 @@ def traffic_record(kind):
 
 
 def main():
+    t_start = time.perf_counter()
     a = parse()
     if a.impl == "reference":
         return reference_arm(a)
@@ -505,25 +506,35 @@ def main():
 
         def brief(r):
             keep = ("label", "wall_s", "iterations", "outer", "rtol", "relres", "floor", "at_floor", "relerr",
-                    "meets_1e-8", "status_text", "ms_per_iteration", "nrhs", "setup_s")
+                    "meets_1e-8", "status_text", "ms_per_iteration", "gb_per_iteration", "gbs", "nrhs", "setup_s")
             out = {"reference": r["reference"], "solves": [{k: x[k] for k in keep if k in x} for x in r["solves"]]}
             if "amg" in r:
                 out["amg_setup"] = r["amg"]
             return out
 
-        r3 = study.c3_study(device=dev, peak_gbs=peak)
+        phases = {}
+
+        def timed(name, fn):
+            t = time.perf_counter()
+            r = fn()
+            phases[name] = round(time.perf_counter() - t, 1)
+            print(f"[bench] {name}: {phases[name]} s", file=sys.stderr, flush=True)
+            return r
+
+        r3 = timed("c3_study", lambda: study.c3_study(device=dev, peak_gbs=peak))
         sol = {"c3": brief(r3)}
         sol["c3"]["spmv"] = r3["spmv"]
-        r4, net = study.c4_study(device=dev)
+        r4, net = timed("c4_study", lambda: study.c4_study(device=dev))
         sol["c4"] = brief(r4)
-        for k in ("training", "inference_s", "gain"):
+        for k in ("training", "smoother_training", "inference_s", "mlp", "gain"):
             if k in r4:
                 sol["c4"][k] = r4[k]
         if not a.no_c5:
-            r5 = study.c5_study(net, device=dev, include_fp64=False, maxit=1000)
+            r5 = timed("c5_study", lambda: study.c5_study(net, device=dev, include_fp64=False, maxit=1000))
             sol["c5"] = brief(r5)
             sol["c5"]["workload"] = r5["workload"]
-        sol["modal_c1"] = study.modal_study("c1", num_eigen=100, num_block=10, device=dev)
+        sol["modal_c1"] = timed("modal_c1", lambda: study.modal_study("c1", num_eigen=100, num_block=10, device=dev))
+        sol["bench_phases_s"] = phases
         line["solve"] = sol
 
     # -- CPU baseline (rank 0, N = 1): the reference algorithm's C port on the same mesh ---------
@@ -567,6 +578,7 @@ def main():
     line["native_so_loaded"] = native_libraries()
     if rank == 0:
         print(json.dumps(line), flush=True)
+        print(f"[bench] total: {time.perf_counter() - t_start:.1f} s", file=sys.stderr, flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 

@@ -227,6 +227,55 @@ def spmv_bytes(n, nnzb, value_bytes, nrhs=1):
     return 9 * value_bytes * nnzb + 4 * nnzb + 4 * (n + 1) + 2 * 3 * n * value_bytes * nrhs
 
 
+def pcg_iteration_bytes(n, nnzb, value_bytes):
+    """Algorithmic HBM bytes of one block-Jacobi PCG iteration: the product with K, the
+    block-diagonal apply (9 values per node) and ~10 passes over the 3N-vectors."""
+    return spmv_bytes(n, nnzb, value_bytes) + 9 * value_bytes * n + 10 * 3 * n * value_bytes
+
+
+def bf16_peak_tflops():
+    import json
+    import os
+    f = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(f) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def mlp_rates(net, S: DeviceSystem, reps=10):
+    """CUDA-event times of the MLP forward (tcgen05) and of its tensor-core backward on the
+    nodes of S; FLOPs of the padded 16 -> 64 -> 64 -> 16 layers the tensor cores compute."""
+    from fem_taichi_gb300.learned import N_HID, N_IN, N_OUT
+    X = NodeData(S, with_probes=False).X
+    n = int(X.shape[0])
+    out, z1, z2 = net.forward(X, save=True)
+    dout = torch.randn(out.shape, device=out.device, dtype=out.dtype) * 1e-3
+    stream = torch.cuda.current_stream(S.device)
+    res = {}
+    for name, fn in (("forward", lambda: net.forward(X)), ("backward", lambda: net.backward(X, z1, z2, dout))):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[name + "_ms"] = e0.elapsed_time(e1) / reps
+    peak, kind = bf16_peak_tflops()
+    fl = 2.0 * n * (N_IN * N_HID + N_HID * N_HID + N_HID * N_OUT)
+    tf = fl / (res["forward_ms"] * 1e-3) / 1e12
+    res.update({"nodes": n, "forward_flops": fl, "forward_tflops": tf, "bf16_peak_tflops": peak, "peak_kind": kind,
+                "frac_bf16": tf / peak,
+                "backward_weight_gradient_flops": fl,
+                "note": "per-node MLP: small matrices (K = 16 / 64), a memory- and latency-bound use of the "
+                        "tensor cores; a small share of the solve"})
+    return res
+
+
 def spmv_rates(S: DeviceSystem, reps=20, peak_gbs=None):
     """CUDA-event time of the autotuned FP64 and FP32 (row-SoA) SpMV on this system's K."""
     out = {}
@@ -286,6 +335,10 @@ def c3_study(device="cuda", rtol=1e-10, peak_gbs=None):
                            ("fp64_amg", dict(rtol=rtol, mixed=False, precond="amg"))], amg=amg)
     for r in rows:
         r["ms_per_iteration"] = 1e3 * r["wall_s"] / max(r["iterations"], 1)
+        if r["label"].endswith("_bj"):
+            b = pcg_iteration_bytes(S.n, S.nnzb, 4 if r["label"].startswith("mixed") else 8)
+            r["gb_per_iteration"] = b / 1e9
+            r["gbs"] = b / (r["ms_per_iteration"] * 1e-3) / 1e9
     return {"workload": "c3 100x100x20 (4:1), 214,221 nodes", "reference": ref, "solves": rows,
             "amg": amg, "spmv": spmv_rates(S, peak_gbs=peak_gbs)}
 
@@ -321,6 +374,7 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32, smooth
     Pl = net.blocks(S)
     torch.cuda.synchronize()
     t_inf = time.perf_counter() - t
+    mlp = mlp_rates(net, S)
     amg = amg_setup(S)
     Fm = face_rhs(S, P, S.F, nrhs, "zmax", seed=4)
     Urm, ref = reference_solution(S, F=Fm, check_cols=[0, 1, 2, 3])
@@ -358,7 +412,8 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32, smooth
         gain["learned_smoother_vs_amg" + suffix] = {"iterations": ls["iterations"] / max(da["iterations"], 1),
                                                    "wall": ls["wall_s"] / da["wall_s"]}
     return {"workload": "c4 eval 160x160x20, 544,341 nodes, 1 and %d RHS" % nrhs, "training": info,
-            "smoother_training": sm_info, "inference_s": t_inf, "reference": ref, "solves": rows, "amg": amg,
+            "smoother_training": sm_info, "inference_s": t_inf, "mlp": mlp, "reference": ref, "solves": rows,
+            "amg": amg,
             "gain": gain}, net
 
 

@@ -158,43 +158,49 @@ __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams 
 }
 
 // Eigenvalues of the symmetric 3x3 [[a00,a01,a02],[a01,a11,a12],[a02,a12,a22]] by cyclic
-// Jacobi rotations (capped at 32 sweeps), returned descending.
+// Jacobi rotations in Rutishauser's form (the rotated off-diagonal set to zero, the diagonal
+// updated as a_pp - t a_pq and a_qq + t a_pq, the third row rotated with tau = s / (1 + c);
+// Numerical Recipes, "jacobi"), off-diagonals negligible against both diagonals dropped after
+// four sweeps; capped at 32 sweeps; returned descending.
 __device__ void sym3_eig_desc(double a00, double a11, double a22, double a01, double a12, double a02,
                               double& p1, double& p2, double& p3) {
-    double a[3][3] = {{a00, a01, a02}, {a01, a11, a12}, {a02, a12, a22}};
+    double d[3] = {a00, a11, a22};
+    double o01 = a01, o02 = a02, o12 = a12;
     for (int sweep = 0; sweep < 32; ++sweep) {
-        const double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-        const double dia = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
-        if (off == 0.0 || off <= 1e-300 || off < 1e-17 * dia) break;
+        if (fabs(o01) + fabs(o02) + fabs(o12) == 0.0) break;
 #pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
-            const int pp = pq == 2 ? 1 : 0;
-            const int qq = pq == 0 ? 1 : 2;
-            const double apq = a[pp][qq];
+            // (p, q, r): (0, 1, 2), (0, 2, 1), (1, 2, 0)
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            double& apq = pq == 0 ? o01 : pq == 1 ? o02 : o12;
+            double& apr = pq == 0 ? o02 : pq == 1 ? o01 : o01;   // (p, r)
+            double& aqr = pq == 0 ? o12 : pq == 1 ? o12 : o02;   // (q, r)
             if (apq == 0.0) continue;
-            const double theta = (a[qq][qq] - a[pp][pp]) / (2.0 * apq);
-            double tt;
-            if (fabs(theta) > 1e150) {
-                tt = 0.5 / theta;
+            const double g = 100.0 * fabs(apq);
+            if (sweep > 3 && fabs(d[p]) + g == fabs(d[p]) && fabs(d[q]) + g == fabs(d[q])) {
+                apq = 0.0;
+                continue;
+            }
+            const double h = d[q] - d[p];
+            double t;
+            if (fabs(h) + g == fabs(h)) {
+                t = apq / h;
             } else {
-                tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double theta = 0.5 * h / apq;
+                t = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
+                if (theta < 0.0) t = -t;
             }
-            const double c = 1.0 / sqrt(tt * tt + 1.0), sn = tt * c;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const double akp = a[k][pp], akq = a[k][qq];
-                a[k][pp] = c * akp - sn * akq;
-                a[k][qq] = sn * akp + c * akq;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const double apk = a[pp][k], aqk = a[qq][k];
-                a[pp][k] = c * apk - sn * aqk;
-                a[qq][k] = sn * apk + c * aqk;
-            }
+            const double c = 1.0 / sqrt(1.0 + t * t), sn = t * c, tau = sn / (1.0 + c);
+            const double ht = t * apq;
+            d[p] -= ht;
+            d[q] += ht;
+            apq = 0.0;
+            const double x = apr, y = aqr;  // rotate (p, r) and (q, r)
+            apr = x - sn * (y + x * tau);
+            aqr = y + sn * (x - y * tau);
         }
     }
-    double e0 = a[0][0], e1 = a[1][1], e2 = a[2][2], tmp;
+    double e0 = d[0], e1 = d[1], e2 = d[2], tmp;
     if (e0 < e1) tmp = e0, e0 = e1, e1 = tmp;
     if (e1 < e2) tmp = e1, e1 = e2, e2 = tmp;
     if (e0 < e1) tmp = e0, e0 = e1, e1 = tmp;

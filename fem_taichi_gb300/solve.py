@@ -85,9 +85,10 @@ class AmgHierarchy:
         self.upload_s = time.perf_counter() - t0
 
     @classmethod
-    def on_device(cls, system, **opts):
+    def on_device(cls, system, host_pattern=True, **opts):
         """Set up from ``system.A64`` and the model's device coordinates; the host pattern of
-        the model (``Physics.SmNode`` / ``ReNode``) saves downloading it."""
+        the model (``Physics.SmNode`` / ``ReNode``) saves downloading it (host_pattern=False:
+        the setup downloads it)."""
         import time
         self = cls.__new__(cls)
         self.lib = system.lib
@@ -97,7 +98,7 @@ class AmgHierarchy:
         P = system.model.Physics
         ip = np.ascontiguousarray(P.SmNode, dtype=np.int32)
         ix = np.ascontiguousarray(P.ReNode, dtype=np.int32)
-        if ip.shape[0] != system.n + 1 or ix.shape[0] != system.nnzb:
+        if not host_pattern or ip.shape[0] != system.n + 1 or ix.shape[0] != system.nnzb:
             ip = ix = None
         h = ctypes.c_void_p()
         torch.cuda.synchronize(system.device)

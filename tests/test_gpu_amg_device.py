@@ -125,3 +125,15 @@ def test_device_setup_edge_cases_bit_identical(case):
     finally:
         Hd.close()
         Hh.close()
+
+
+def test_device_setup_without_a_host_pattern(pair):
+    """The level-0 pattern downloaded by the setup itself (no host copy given) builds the same
+    hierarchy bit for bit."""
+    P, M, S, Hd, Hh = pair
+    from fem_taichi_gb300.solve import AmgHierarchy
+    Hn = AmgHierarchy.on_device(S, host_pattern=False, max_coarse=200)
+    try:
+        _same(_exports(Hn), _exports(Hd))
+    finally:
+        Hn.close()
