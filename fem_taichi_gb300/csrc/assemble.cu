@@ -18,7 +18,9 @@
 //     load (FEM_model_bsr.py:229-245) is F_a = sum_g DE det_g N_a(g) W x(g); W x is linear and
 //     the isoparametric map reproduces it at the Gauss points, W x(g) = sum_b N_b(g) W x_b, so
 //     F_a = sum_b M_ab W x_b: the same quantity from the mass blocks, with no per-Gauss-point
-//     load density.  Each element writes one 3 KB record: 36 x (K 3x3 + M) and 8 x F(3).
+//     load density.  Each element writes one 2,944-byte record: 28 off-diagonal pairs as
+//     K (3x3) + M, 8 diagonal pairs as the 6 distinct values of the symmetric K + M (8-double
+//     slots), 8 x F(3).
 //
 //  2. k_gather -- one warp per block row i.  Lane l owns slot l of the row (column node
 //     indices[indptr[i] + l]).  The warp walks the incident (element, corner) list of
@@ -37,10 +39,22 @@ namespace {
 
 constexpr int kEpc = 16;                 // elements per CTA in the element kernel
 constexpr int kElemThreads = kEpc * 8;   // 8 threads per element
-constexpr int kRec = 384;                // doubles per element record
-constexpr int kPairStride = 10;          // K (9) + M (1)
-constexpr int kFOff = 36 * kPairStride;  // 360: F block offset within a record
-constexpr int kRPad = 25;                // padded row (24 used) to spread smem banks
+// Element record (FP64 kernels), 368 doubles = 2,944 bytes: for each corner a in turn, the
+// diagonal pair (a, a) as the 6 distinct values of the symmetric K_aa (00, 11, 22, 01, 02, 12)
+// + M_aa in an 8-double slot, then the pairs (a, b), b = a + 1..7, as K_ab (3x3) + M_ab; then
+// F (8 x 3).  The blocks the 8 lanes of a row read for one incident entry, (a, a..7), stay
+// contiguous; every block starts on a 16-byte boundary.
+constexpr int kPairStride = 10;   // K (9) + M (1) of an off-diagonal pair
+constexpr int kDiagStride = 8;    // K_aa (6) + M_aa + 1 unused
+constexpr int kFOff = 8 * kDiagStride + 28 * kPairStride;  // 344: F block offset within a record
+constexpr int kRec = kFOff + 24;  // 368 doubles per element record
+constexpr int kRPad = 25;         // padded row (24 used) to spread smem banks
+
+// record offset of pair (lo, hi), lo <= hi: 10 doubles per pair in upper-triangular order, less
+// 2 for every diagonal slot before it
+__host__ __device__ constexpr int pair_offset(int lo, int hi) {
+    return kPairStride * (lo * 8 - (lo * (lo - 1)) / 2 + (hi - lo)) - 2 * (lo + (hi > lo ? 1 : 0));
+}
 
 struct ElemParams {
     const double* xyz;
@@ -89,7 +103,7 @@ __device__ __forceinline__ void offdiag_pair(int q, int& a, int& b) {
     b = aa + 1 + rem;
 }
 
-__global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams p) {
+__global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ElemSmem& s = *reinterpret_cast<ElemSmem*>(smem_raw);
     const int tid = threadIdx.x;
@@ -186,15 +200,16 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
             m = fma(s.det[el][g], s.nn[pi][g], m);
         }
         const double lm = lam + mu;
-        double* o = rec + pi * kPairStride;
+        double* o = rec + kPairStride * pi - 2 * a;  // pair_offset(a, a)
         o[0] = D0d * P00 + mu * (P11 + P22);
-        o[4] = D0d * P11 + mu * (P00 + P22);
-        o[8] = D0d * P22 + mu * (P00 + P11);
-        o[1] = o[3] = lm * P01;
-        o[2] = o[6] = lm * P02;
-        o[5] = o[7] = lm * P12;
-        o[9] = DE * m;
-        s.m[el][pi] = o[9];
+        o[1] = D0d * P11 + mu * (P00 + P22);
+        o[2] = D0d * P22 + mu * (P00 + P11);
+        o[3] = lm * P01;
+        o[4] = lm * P02;
+        o[5] = lm * P12;
+        o[6] = DE * m;
+        o[7] = 0.0;  // the unused slot: whole 32-byte sectors written, none read back from DRAM
+        s.m[el][pi] = o[6];
     }
     // off-diagonal pairs
     for (int q = t; q < 28 && valid; q += 8) {
@@ -218,7 +233,7 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
             P[2][2] = fma(q2, r2, P[2][2]);
             m = fma(s.det[el][g], s.nn[pi][g], m);
         }
-        double* o = rec + pi * kPairStride;
+        double* o = rec + kPairStride * pi - 2 * (a + 1);  // pair_offset(a, b), a < b
         o[0] = D0d * P[0][0] + mu * (P[1][1] + P[2][2]);
         o[4] = D0d * P[1][1] + mu * (P[0][0] + P[2][2]);
         o[8] = D0d * P[2][2] + mu * (P[0][0] + P[1][1]);
@@ -247,6 +262,34 @@ __global__ void __launch_bounds__(kElemThreads) k_hex8_element(const ElemParams 
         rec[kFOff + 3 * t + 1] = f1;
         rec[kFOff + 3 * t + 2] = f2;
     }
+}
+
+// Block (a, b) of element e as 10 doubles (K row-major, then M), oriented for row corner a and
+// column corner b: an off-diagonal pair is stored once (a < b) and transposed for a > b; a
+// diagonal pair is stored as its 6 distinct values.  Every lane issues the same five 16-byte
+// loads (a diagonal slot's last two land in the next block or in F and go unused) and picks
+// its values with selects, so the lanes of a row do not diverge.
+__device__ __forceinline__ void load_pair_block(const double* rec, int64_t e, int a, int b, double (&v)[kPairStride]) {
+    const bool dg = a == b, tr = a > b;
+    const int lo = min(a, b), hi = max(a, b);
+    const double2* blk = reinterpret_cast<const double2*>(rec + e * kRec + pair_offset(lo, hi));
+    double w[kPairStride];
+#pragma unroll
+    for (int q = 0; q < kPairStride / 2; ++q) {
+        const double2 x = __ldg(blk + q);
+        w[2 * q] = x.x;
+        w[2 * q + 1] = x.y;
+    }
+    v[0] = w[0];
+    v[1] = dg ? w[3] : (tr ? w[3] : w[1]);
+    v[2] = dg ? w[4] : (tr ? w[6] : w[2]);
+    v[3] = dg ? w[3] : (tr ? w[1] : w[3]);
+    v[4] = dg ? w[1] : w[4];
+    v[5] = dg ? w[5] : (tr ? w[7] : w[5]);
+    v[6] = dg ? w[4] : (tr ? w[2] : w[6]);
+    v[7] = dg ? w[5] : (tr ? w[5] : w[7]);
+    v[8] = dg ? w[2] : w[8];
+    v[9] = dg ? w[6] : w[9];
 }
 
 struct GatherParams {
@@ -297,20 +340,10 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams p) {
             while (mask) {
                 const int b = __ffs(mask) - 1;
                 mask &= mask - 1;
-                const int lo = min(a, b), hi = max(a, b);
-                const double2* blk = reinterpret_cast<const double2*>(p.rec + e * kRec + pair_index(lo, hi) * kPairStride);
-                const double2 v0 = __ldg(blk), v1 = __ldg(blk + 1), v2 = __ldg(blk + 2), v3 = __ldg(blk + 3),
-                              v4 = __ldg(blk + 4);
-                double v[10] = {v0.x, v0.y, v1.x, v1.y, v2.x, v2.y, v3.x, v3.y, v4.x, v4.y};
-                if (a <= b) {
+                double v[kPairStride];
+                load_pair_block(p.rec, e, a, b, v);
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) acc[k] += v[k];
-                } else {
-#pragma unroll
-                    for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-                        for (int qq = 0; qq < 3; ++qq) acc[3 * pp + qq] += v[3 * qq + pp];
-                }
+                for (int k = 0; k < 9; ++k) acc[k] += v[k];
                 accm += v[9];
             }
         }
@@ -397,25 +430,6 @@ struct Gather64Smem {
     double acc[kG64Warps][kG64Rows][kG64RowStride];
     int cols[kG64Warps][kG64Rows][kG64MaxL];
 };
-
-// Block (a, b) of element e as 10 doubles (K row-major, then M); the record stores a <= b.
-__device__ __forceinline__ void load_pair_block(const double* rec, int64_t e, int a, int b, double (&v)[kPairStride]) {
-    const int lo = min(a, b), hi = max(a, b);
-    const double2* blk = reinterpret_cast<const double2*>(rec + e * kRec + pair_index(lo, hi) * kPairStride);
-    double w[kPairStride];
-#pragma unroll
-    for (int q = 0; q < kPairStride / 2; ++q) {
-        const double2 x = __ldg(blk + q);
-        w[2 * q] = x.x;
-        w[2 * q + 1] = x.y;
-    }
-    const bool tr = a > b;
-#pragma unroll
-    for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-        for (int qq = 0; qq < 3; ++qq) v[3 * pp + qq] = tr ? w[3 * qq + pp] : w[3 * pp + qq];
-    v[9] = w[9];
-}
 
 __device__ __forceinline__ int find_slot64(const int* cols, int L, int node) {
     int lo = 0, hi = L - 1;
@@ -666,7 +680,7 @@ int check_mesh(const fem_mesh* m) {
 using namespace fem;
 
 extern "C" size_t fem_assemble_workspace_bytes(int64_t n_elem) {
-    // FEM_ALGO_FP64: one 3,072-byte record per element; FEM_ALGO_DD: eight 672-byte
+    // FEM_ALGO_FP64: one 2,944-byte record per element; FEM_ALGO_DD: eight 672-byte
     // row-ordered chunks per element.  The larger of the two serves both.
     return n_elem > 0 ? size_t(n_elem) * 8 * 672 : 0;
 }
