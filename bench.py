@@ -456,8 +456,12 @@ def main():
             del r
         torch.cuda.synchronize()
         w1 = max_over_ranks(time.perf_counter() - w0, dev)
+        staged = getattr(model, "m_staging", True)
         line["e2e"] = {"value": whole_job_rate(ws, E * ne, w1), "unit": UNIT, "h2d_bytes_per_step": 24 * N,
-                       "d2h_bytes_per_step": 72 * nnzb + 24 * nnzb + 24 * N, "steps": ne,
+                       # K (9 per block) + M (1 per block when staged, else the 3 of the CSR) + F
+                       "d2h_bytes_per_step": 72 * nnzb + (8 if staged else 24) * nnzb + 24 * N, "steps": ne,
+                       "host_writes_per_step": 72 * nnzb + 24 * nnzb + 24 * N,
+                       "parts": model.pipeline_parts,
                        "ms_per_step": w1 / ne * 1e3, "arith": "FP64",
                        "path": "Model.set_coordinates(pinned) + Get_MatrixKL + Get_MatrixM + Get_VectorF",
                        "gpu_launches": 2 * ne * model.pipeline_parts}

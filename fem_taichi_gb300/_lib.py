@@ -113,6 +113,9 @@ SIGNATURES = {
                                       c_size_t, c_void_p]),
     "fem_assemble_gather": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemAssemblyOut), c_void_p, c_size_t,
                                     c_void_p]),
+    "fem_assemble_host_staged": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial),
+                                         ctypes.POINTER(FemAssemblyOut), c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "fem_assemble_host": (c_int, [ctypes.POINTER(FemMesh), ctypes.POINTER(FemMaterial), ctypes.POINTER(FemAssemblyOut),
                                   c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_size_t, c_void_p]),

@@ -848,10 +848,17 @@ extern "C" int fem_assemble(const fem_mesh* mesh, const fem_material* mat, const
     return fem_assemble_gather(mesh, out, workspace, workspace_bytes, stream);
 }
 
-extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
-                                 const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
-                                 int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
-                                 size_t workspace_bytes, void* stream) {
+namespace fem {
+namespace {
+
+// fem_assemble_host; with `on_part`, the calling thread also waits for each part's copies in
+// turn and calls on_part(q) while later parts are still being copied (then returns only when
+// every copy and every on_part call is done).
+template <typename OnPart>
+int assemble_host_impl(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                       const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split, int n_parts,
+                       double* K_host, double* M_host, double* F_host, void* workspace, size_t workspace_bytes,
+                       void* stream, OnPart* on_part) {
     int rc = check_assembly_inputs(mesh, mat, workspace, workspace_bytes);
     if (rc) return rc;
     FEM_REQUIRE(out != nullptr, "out is NULL");
@@ -876,11 +883,13 @@ extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, 
     cudaStream_t st = as_stream(stream);
     const bool dd = out->algo == FEM_ALGO_DD;
     const int parts = n_parts;
-    std::vector<cudaEvent_t> done(parts, nullptr);
+    std::vector<cudaEvent_t> done(parts, nullptr), copied(parts, nullptr);
     cudaStream_t cs = nullptr;
     cudaEvent_t fin = nullptr;
     auto cleanup = [&] {
         for (cudaEvent_t e : done)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : copied)
             if (e) cudaEventDestroy(e);
         if (fin) cudaEventDestroy(fin);
         if (cs) cudaStreamDestroy(cs);
@@ -925,13 +934,65 @@ extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, 
             (e = cudaMemcpyAsync(F_host + 3 * r0, out->F + 3 * r0, sizeof(double) * 3 * (r1 - r0),
                                  cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
             return fail(e, "F device->host copy");
+        if (on_part && ((e = cudaEventCreateWithFlags(&copied[q], cudaEventDisableTiming)) != cudaSuccess ||
+                        (e = cudaEventRecord(copied[q], cs)) != cudaSuccess))
+            return fail(e, "copy event");
     }
+    if (on_part)
+        for (int q = 0; q < parts; ++q) {
+            if ((e = cudaEventSynchronize(copied[q])) != cudaSuccess) return fail(e, "copy event wait");
+            (*on_part)(q);
+        }
     // the caller's stream is ordered after the last copy
     if ((e = cudaEventCreateWithFlags(&fin, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventRecord(fin, cs)) != cudaSuccess || (e = cudaStreamWaitEvent(st, fin, 0)) != cudaSuccess)
         return fail(e, "copy completion event");
     cleanup();
     return FEM_OK;
+}
+
+}  // namespace
+}  // namespace fem
+
+extern "C" int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                                 const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
+                                 int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+    struct NoPart {
+        void operator()(int) const {}
+    };
+    return assemble_host_impl<NoPart>(mesh, mat, out, row_split, elem_split, block_split, n_parts, K_host, M_host,
+                                      F_host, workspace, workspace_bytes, stream, nullptr);
+}
+
+extern "C" int fem_assemble_host_staged(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                                        const int64_t* row_split, const int64_t* elem_split,
+                                        const int64_t* block_split, int n_parts, const int32_t* indptr_host,
+                                        double* K_host, double* M_host, double* F_host, double* M_stage,
+                                        void* workspace, size_t workspace_bytes, void* stream) {
+    FEM_REQUIRE(out != nullptr && mesh != nullptr, "NULL argument");
+    if (!M_host || !M_stage || out->m_layout != FEM_LAYOUT_CSR)
+        return fem_assemble_host(mesh, mat, out, row_split, elem_split, block_split, n_parts, K_host, M_host,
+                                 F_host, workspace, workspace_bytes, stream);
+    FEM_REQUIRE(indptr_host != nullptr && row_split != nullptr && n_parts >= 1, "NULL argument");
+    // M leaves the device as one value per block (the BSR layout) into M_stage; the reference's
+    // scalar CSR (3 copies of it per block row) is written on the host, part by part, while
+    // the later parts are still being copied.
+    fem_assembly_out o = *out;
+    o.m_layout = FEM_LAYOUT_BSR;
+    auto expand = [&](int q) {
+        const int64_t r0 = row_split[q], r1 = row_split[q + 1];
+#pragma omp parallel for schedule(dynamic, 512)
+        for (int64_t i = r0; i < r1; ++i) {
+            const int64_t rs = indptr_host[i], L = indptr_host[i + 1] - rs;
+            const double* src = M_stage + rs;
+            double* dst = M_host + 3 * rs;
+            for (int pp = 0; pp < 3; ++pp)
+                for (int64_t l = 0; l < L; ++l) dst[pp * L + l] = src[l];
+        }
+    };
+    return assemble_host_impl(mesh, mat, &o, row_split, elem_split, block_split, n_parts, K_host, M_stage, F_host,
+                              workspace, workspace_bytes, stream, &expand);
 }
 
 extern "C" int fem_csr_index(const fem_mesh* mesh, int32_t* rowK, int32_t* colK, int32_t* rowM, int32_t* colM,

@@ -138,7 +138,8 @@ class Model:
         self._cache = None         # (version, {"K", "M", "F"} host arrays not yet handed out)
         self._plan = None
         self.U = None              # large-displacement state (LDinit)
-        self.pipeline_parts = 8    # parts of fem_assemble_host (copies overlap the next part)
+        self.pipeline_parts = 16   # parts of fem_assemble_host (copies overlap the next part)
+        self.m_staging = True      # M leaves the device as one value per block (fem_assemble_host_staged)
         if algo not in ("dd", "fp64"):
             raise ValueError("algo must be 'dd' or 'fp64'")
         self.algo = algo
@@ -216,7 +217,9 @@ class Model:
     def assemble_host(self, n_parts=None):
         """One assembly pass delivered to page-locked host arrays: K (9*nnzb,) and M (3*nnzb,)
         in the reference CSR orders, F (3N,).  The device->host copies of each part of the
-        block rows overlap the kernels of the next part (fem_assemble_host)."""
+        block rows overlap the kernels of the next part; M leaves the device as one value per
+        block and is written in the CSR order on the host while later parts are copied
+        (fem_assemble_host_staged)."""
         d = self.device
         nnzb = self.mesh.nnzb
         Kd = torch.empty(9 * nnzb, dtype=torch.float64, device=d)
@@ -230,12 +233,27 @@ class Model:
                            self.fixed.data_ptr(), self.loads.data_ptr(),
                            _lib.ALGO_DD if self.algo == "dd" else _lib.ALGO_FP64)
         rs, es, bs = self.pipeline_plan(n_parts)
-        _lib.check(self.lib.fem_assemble_host(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), ctypes.byref(o),
-                                              rs.ctypes.data, es.ctypes.data, bs.ctypes.data, len(rs) - 1,
-                                              Kh.data_ptr(), Mh.data_ptr(), Fh.data_ptr(), _dptr(ws), ws.numel(),
-                                              _stream(d)), "fem_assemble_host")
+        if not self.m_staging:
+            _lib.check(self.lib.fem_assemble_host(ctypes.byref(self.mesh.c), ctypes.byref(self.mat), ctypes.byref(o),
+                                                  rs.ctypes.data, es.ctypes.data, bs.ctypes.data, len(rs) - 1,
+                                                  Kh.data_ptr(), Mh.data_ptr(), Fh.data_ptr(), _dptr(ws), ws.numel(),
+                                                  _stream(d)), "fem_assemble_host")
+            torch.cuda.current_stream(d).synchronize()
+            return Kh.numpy(), Mh.numpy(), Fh.numpy()
+        Ms = torch.empty(nnzb, dtype=torch.float64, pin_memory=True)   # M, one value per block
+        ind = self._indptr_host()
+        _lib.check(self.lib.fem_assemble_host_staged(ctypes.byref(self.mesh.c), ctypes.byref(self.mat),
+                                                     ctypes.byref(o), rs.ctypes.data, es.ctypes.data, bs.ctypes.data,
+                                                     len(rs) - 1, ind.ctypes.data, Kh.data_ptr(), Mh.data_ptr(),
+                                                     Fh.data_ptr(), Ms.data_ptr(), _dptr(ws), ws.numel(), _stream(d)),
+                   "fem_assemble_host_staged")
         torch.cuda.current_stream(d).synchronize()
         return Kh.numpy(), Mh.numpy(), Fh.numpy()
+
+    def _indptr_host(self):
+        if getattr(self, "_indptr_h", None) is None:
+            self._indptr_h = np.ascontiguousarray(self.Physics.SmNode, dtype=np.int32)
+        return self._indptr_h
 
     def set_coordinates(self, xyz) -> None:
         """Move the nodes (same topology); the next getter re-assembles."""

@@ -164,6 +164,17 @@ int fem_assemble_host(const fem_mesh* mesh, const fem_material* mat, const fem_a
                       const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
                       int n_parts, double* K_host, double* M_host, double* F_host, void* workspace,
                       size_t workspace_bytes, void* stream);
+/* fem_assemble_host for getters that return M in the reference's scalar CSR (out->m_layout =
+ * FEM_LAYOUT_CSR): M leaves the device as one value per block into M_stage (HOST, nnzb
+ * doubles, page-locked) instead of three, and the calling thread writes M_host in the CSR
+ * order from it, part by part, while the later parts are still being copied; indptr_host is
+ * the host copy of the block row pointers.  Returns when K_host, M_host and F_host are complete.
+ * With M_stage or M_host NULL, or a BSR M, it is fem_assemble_host. */
+int fem_assemble_host_staged(const fem_mesh* mesh, const fem_material* mat, const fem_assembly_out* out,
+                             const int64_t* row_split, const int64_t* elem_split, const int64_t* block_split,
+                             int n_parts, const int32_t* indptr_host, double* K_host, double* M_host,
+                             double* F_host, double* M_stage, void* workspace, size_t workspace_bytes,
+                             void* stream);
 /* Plan of fem_assemble_host (host arrays, no reference counterpart): row_split[0..n_parts]
  * splits the block rows into parts of about nnzb / n_parts blocks; block_split[q] =
  * indptr[row_split[q]]; elem_split[q + 1] = 1 + the largest element incident to a row below
