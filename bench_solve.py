@@ -514,6 +514,24 @@ def modal_study(cfg="c1", num_eigen=100, num_block=10, device="cuda", precond="a
             "lowest_freq_hz": [float(f) for f in freq[:5]], "M_orthonormality_err": orth}
 
 
+def profile_setup(cfg="c5"):
+    """One device multigrid setup (after a warm one) bracketed by cudaProfilerStart/Stop, for
+    launch-list captures with ``ncu --profile-from-start off``:
+    ``python bench_solve.py --profile-setup c5``."""
+    P = _mesh.config_mesh(cfg)
+    S = DeviceSystem(Model(cfg, P, STEEL))
+    S.amg_variant().close()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t = time.perf_counter()
+    H = S.amg_variant()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t
+    torch.cuda.profiler.stop()
+    print({"setup_s": wall, "phases_s": H.setup_phases(), "levels": _levels(H)})
+    H.close()
+
+
 def profile_solve(cfg="c3", nrhs=1):
     """One warm multigrid-preconditioned FP64 static solve bracketed by cudaProfilerStart/Stop,
     for launch-list captures with ``ncu --profile-from-start off``:
@@ -536,6 +554,8 @@ if __name__ == "__main__":
     import sys
     if len(sys.argv) >= 2 and sys.argv[1] == "--profile":
         profile_solve(sys.argv[2] if len(sys.argv) > 2 else "c3", int(sys.argv[3]) if len(sys.argv) > 3 else 1)
+    elif len(sys.argv) >= 2 and sys.argv[1] == "--profile-setup":
+        profile_setup(sys.argv[2] if len(sys.argv) > 2 else "c5")
     elif len(sys.argv) >= 2 and sys.argv[1] == "--c5-check":
         import json
         print(json.dumps(c5_independent_check(maxit=int(sys.argv[2]) if len(sys.argv) > 2 else 150_000)))

@@ -198,6 +198,41 @@ def test_host_pipeline_equals_device_assembly(algo, order):
     assert np.array_equal(Kp, Kd) and np.array_equal(Mp, Md) and np.array_equal(Fp, Fd)
 
 
+@pytest.mark.parametrize("algo", ALGOS)
+def test_staged_host_pipeline_equals_device_assembly(algo):
+    """fem_assemble_host_staged (M over the link as one value per block, written in the
+    reference CSR order on the host part by part) returns the device assembly's CSR K, M, F bit
+    for bit, into pageable numpy buffers, for 1 and 5 parts."""
+    import ctypes
+    from fem_taichi_gb300 import _lib
+    from fem_taichi_gb300.model import _dptr, _stream
+    P = F.hex_block(11, 7, 6, jitter=0.1, seed=9, fix="zmin", load_face="zmax", load=(1.0, 0, -2.0))
+    M = F.Model("s", P, STEEL, algo=algo)
+    Kd, Md, Fd = M.assemble(k_layout="csr", m_layout="csr")
+    torch.cuda.synchronize()
+    Kd, Md, Fd = Kd.cpu().numpy(), Md.cpu().numpy(), Fd.cpu().numpy().reshape(-1)
+    L = _lib.load()
+    nnzb = M.mesh.nnzb
+    ind = np.ascontiguousarray(P.SmNode, dtype=np.int32)
+    for parts in (1, 5):
+        Kt = torch.empty(9 * nnzb, dtype=torch.float64, device="cuda")
+        Mt = torch.empty(3 * nnzb, dtype=torch.float64, device="cuda")
+        Ft = torch.empty(3 * P.Num_Node, dtype=torch.float64, device="cuda")
+        Kp, Mp, Fp = np.full(9 * nnzb, np.nan), np.full(3 * nnzb, np.nan), np.full(3 * P.Num_Node, np.nan)
+        stage = np.full(nnzb, np.nan)
+        o = _lib.FemAssemblyOut(_lib.LAYOUT_CSR, _lib.LAYOUT_CSR, Kt.data_ptr(), Mt.data_ptr(), Ft.data_ptr(),
+                                M.fixed.data_ptr(), M.loads.data_ptr(),
+                                _lib.ALGO_DD if algo == "dd" else _lib.ALGO_FP64)
+        rs, es, bs = M.pipeline_plan(parts)
+        ws = M.workspace()
+        _lib.check(L.fem_assemble_host_staged(ctypes.byref(M.mesh.c), ctypes.byref(M.mat), ctypes.byref(o),
+                                              rs.ctypes.data, es.ctypes.data, bs.ctypes.data, parts, ind.ctypes.data,
+                                              Kp.ctypes.data, Mp.ctypes.data, Fp.ctypes.data, stage.ctypes.data,
+                                              _dptr(ws), ws.numel(), _stream(M.device)), "fem_assemble_host_staged")
+        torch.cuda.synchronize()
+        assert np.array_equal(Kp, Kd) and np.array_equal(Mp, Md) and np.array_equal(Fp, Fd), parts
+
+
 def test_host_pipeline_rejects_bad_plan():
     import ctypes
     from fem_taichi_gb300 import _lib
