@@ -394,13 +394,14 @@ class Static_solver:
                            "converged": res[-1] <= max_errs}
         return U.cpu().numpy()
 
-    def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, stall_window=256, **kw):
+    def Solve_gpu(self, rtol=1e-10, F=None, mixed=True, precond="bj", maxit=50000, stall_window=None, **kw):
         """GPU solve; returns U as numpy ((3N,) or (3N, R)).  precond: 'bj', 'amg' (multigrid
         V-cycle), 'learned' (uses ``self.Model.learned_precond`` (N, 9) if set) or an (N, 9)
         array.  The learned solve runs with a stall detector: when its worst relative residual
-        has not halved within ``stall_window`` iterations (or it fails otherwise) the solve
-        switches to plain block Jacobi from the start; ``last_stats["fallback_from"]`` then
-        holds the abandoned attempt."""
+        has not halved within ``stall_window`` iterations (default 256; or it fails otherwise)
+        the solve switches to plain block Jacobi from the start; ``last_stats["fallback_from"]``
+        then holds the abandoned attempt.  For the other preconditioners ``stall_window`` (default
+        off) ends a stalling solve with FEM_ERR_NOT_CONVERGED."""
         if self.Qtype != 0:
             raise ValueError("Solve_gpu is the linear solve; Qtype=1 uses Solve_cpu / Solve_nonlinear")
         S = self._system()
@@ -418,8 +419,9 @@ class Static_solver:
                 raise ValueError("precond must be 'bj', 'amg', 'learned' or an (N, 9) array")
         else:
             P = precond
-        U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P,
-                        stall_window=stall_window if fallback else 0, **kw)
+        if stall_window is None:
+            stall_window = 256 if fallback else 0
+        U, st = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=P, stall_window=stall_window, **kw)
         if fallback and st["status"] != 0:
             U, st2 = S.solve(F=F, rtol=rtol, maxit=maxit, mixed=mixed, precond=None, **kw)
             st2["fallback_from"] = st
@@ -431,8 +433,9 @@ class Static_solver:
         """SOLVE_static.py:12-75 signature: returns U (3N,).  Qtype 0 runs the GPU linear solve
         to a relative residual of 1e-12 (the reference used a direct factorisation, which
         always returns a solution): mixed block-Jacobi PCG first (capped at 20,000
-        iterations), and when that does not converge (slender or stretched meshes) the FP64
-        multigrid solve with compensated residuals to 1e-12 or as far as FP64 allows;
+        iterations, and abandoned once its residual has not halved in 1,000), and when that does
+        not converge (slender or stretched meshes) the FP64 multigrid solve with compensated
+        residuals to 1e-12 or as far as FP64 allows;
         ``last_stats["fallback_from"]`` then holds the first attempt.  When the fallback also
         stops above 1e-12, a RuntimeWarning gives its residual and the FP64 floor
         (``last_stats["floor"]``): the displacement is then as accurate as FP64 storage permits
@@ -440,7 +443,7 @@ class Static_solver:
         (Solve_nonlinear)."""
         if self.Qtype == 1:
             return self.Solve_nonlinear(max_errs=max_errs, max_iters=max_iters)
-        U = self.Solve_gpu(rtol=1e-12, mixed=True, maxit=20000)
+        U = self.Solve_gpu(rtol=1e-12, mixed=True, maxit=20000, stall_window=1000)
         if self.last_stats["status"] != 0:
             first = self.last_stats
             U = self.Solve_gpu(rtol=1e-12, mixed=False, precond="amg", residual="extra", max_outer=8)

@@ -211,3 +211,4 @@ def test_drop_in_solve_falls_back_to_multigrid_on_the_slab(slab):
     assert st["status"] == _lib.FEM_ERR_NOT_CONVERGED and st["relres"] <= 16 * st["floor"], st
     if "fallback_from" in st:
         assert st["precond"] == "amg" and st["fallback_from"]["status"] != 0
+        assert st["fallback_from"]["iterations"] < 20000, st["fallback_from"]   # left on stalling
