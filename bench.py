@@ -49,10 +49,13 @@ UNIT = "Melem/s"
 # FP64 operations of one element's integrals (FMA = 2), counted from k_hex8_element:
 # W x and element-local coordinates 8 x (15 + 3); trilinear coefficients 24 x 15;
 # per Gauss point J 27 FMA, adjugate 27, det 5, reciprocal ~10, R 24 x 5, R/det 24;
-# 8 diagonal pairs x (8 x 7 FMA + 17); 28 off-diagonal pairs x (8 x 10 FMA + 31);
-# F = M W x 8 x 24 FMA.  ELEM_FP64_INSTR counts instructions (FMA = 1) the same way.
-ELEM_FP64_FLOPS = 8 * 18 + 24 * 15 + 8 * (54 + 27 + 5 + 10 + 120 + 24) + 8 * (112 + 17) + 28 * (160 + 31) + 8 * 48
-ELEM_FP64_INSTR = 8 * 12 + 24 * 8 + 8 * (27 + 18 + 3 + 5 + 72 + 24) + 8 * (56 + 15) + 28 * (80 + 22) + 8 * 24
+# 8 diagonal pairs x (8 x 6 FMA + 16); 28 off-diagonal pairs x (8 x 9 FMA + 30); the mass by
+# sum factorisation 12 x 3 + 18 x 3 + 27 x 4; F = M W x 8 x 24 FMA.  ELEM_FP64_INSTR counts
+# instructions (FMA = 1) the same way.
+ELEM_FP64_FLOPS = (8 * 18 + 24 * 15 + 8 * (54 + 27 + 5 + 10 + 120 + 24) + 8 * (96 + 16) + 28 * (144 + 30)
+                   + (12 * 3 + 18 * 3 + 27 * 4) + 8 * 48)
+ELEM_FP64_INSTR = (8 * 12 + 24 * 8 + 8 * (27 + 18 + 3 + 5 + 72 + 24) + 8 * (48 + 14) + 28 * (72 + 21)
+                   + (12 * 2 + 18 * 2 + 27 * 3) + 8 * 24)
 # FP64 operations of one element of the stress element kernel (k_stress_element): corner 0
 # subtracted 48; trilinear coefficients of x and u 24 x 2 x (7 FMA + 1); per Gauss point J
 # and the displacement gradient 2 x 27 FMA, adjugate 27, det 5, reciprocal ~10, H 9 x 6,

@@ -14,7 +14,9 @@
 //     K_ab[p][p] = D0d P[p][p] + mu (tr P - P[p][p]), which equals sum_g det (B1_a^T D0 B1_b +
 //     B2_a^T D1 B2_b) of the reference (FEM_model_bsr.py:262-274, 303-347) with a different
 //     summation order.  The consistent mass M_ab = DE sum_g det_g N_a N_b
-//     (FEM_model_bsr.py:276-287) uses a table of N_a N_b at the Gauss points.  The centrifugal
+//     (FEM_model_bsr.py:276-287) is sum-factorised: N_a(g) is a product of one 1D factor per
+//     axis, so M_ab depends only on the per-axis class of (a, b) and the 8 det_g are contracted
+//     axis by axis (27 classes, 141 FP64 operations per element instead of 288).  The centrifugal
 //     load (FEM_model_bsr.py:229-245) is F_a = sum_g DE det_g N_a(g) W x(g); W x is linear and
 //     the isoparametric map reproduces it at the Gauss points, W x(g) = sum_b N_b(g) W x_b, so
 //     F_a = sum_b M_ab W x_b: the same quantity from the mass blocks, with no per-Gauss-point
@@ -64,22 +66,32 @@ struct ElemParams {
     double DE, D0d, lam, mu;
     double wc[3][3];   // centrifugal operator: f = wc . x (UnitVectorF)
     DevTables tab;
-    double nn[36][8];  // N_a(g) N_b(g) for pair (a <= b), Gauss point g
+    // tm[s][c]: product of the 1D shape factors of two corners along one axis at a Gauss point
+    // on the negative (s = 0) or positive (s = 1) side: c = 0 both corners negative, 1 mixed,
+    // 2 both positive
+    double tm[2][3];
 };
 
 struct ElemSmem {
     double dnr[8][8][3];
-    double nr[8][8];
-    double nn[36][8];
-    double x[kEpc][8][3];
-    double xl[kEpc][8][3];      // corner coordinates relative to corner 0
+    double x[kEpc][8][3];       // corner coordinates; later the first mass contraction (D1)
+    double xl[kEpc][8][3];      // corner coordinates relative to corner 0; later D2
     double cf[kEpc][8][3];      // trilinear coefficients c_k of the element map (c_0 unused)
     double wx[kEpc][8][3];      // W x_a: centrifugal density per unit mass at corner a
     double R[kEpc][8][kRPad];   // R_a(g)[i] at [el][g][3a+i]
     double Rs[kEpc][8][kRPad];  // R_a(g)[i] / det_g
     double det[kEpc][8];
-    double m[kEpc][36];         // M_ab of the element (DE included)
+    double m[kEpc][36];         // mass by corner-pair class (27 used, DE included), see mass_class
 };
+
+// Class of the corner pair (a, b) for the mass: per axis 0 both corners on the negative side,
+// 1 mixed, 2 both positive (corner sides as in monomial_sign); M_ab depends only on it.
+__device__ __forceinline__ int mass_class(int a, int b) {
+    const int nx = (0x66 >> a) & 1, ny = (0xCC >> a) & 1, nz = (0x0F >> a) & 1;
+    const int mx = (0x66 >> b) & 1, my = (0xCC >> b) & 1, mz = (0x0F >> b) & 1;
+    const int cx = nx != mx ? 1 : (nx ? 0 : 2), cy = ny != my ? 1 : (ny ? 0 : 2), cz = nz != mz ? 1 : (nz ? 0 : 2);
+    return cx * 9 + cy * 3 + cz;
+}
 
 // m_k(corner a) for the trilinear monomials 1, xi, eta, zeta, xi eta, eta zeta, xi zeta,
 // xi eta zeta; corner signs in the reference's node order (FEM_model_bsr.py:371-382):
@@ -113,8 +125,6 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
     const bool valid = e < p.e_end;
 
     for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
-    for (int k = tid; k < 64; k += kElemThreads) (&s.nr[0][0])[k] = (&p.tab.nr[0][0])[k];
-    for (int k = tid; k < 36 * 8; k += kElemThreads) (&s.nn[0][0])[k] = (&p.nn[0][0])[k];
     if (valid) {
         const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
         const int node = __ldg(cn + t);
@@ -180,13 +190,41 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
     }
     __syncthreads();
 
+    // ---- mass, M_ab = DE sum_g det_g N_a(g) N_b(g), by sum factorisation ------------------
+    // N_a(g) is a product of one 1D factor per axis, so M_ab depends on the class of (a, b) per
+    // axis only: contract the 8 det_g along x (D1: 3 classes x 4 (y, z) points), y (D2: 9 x 2),
+    // z (D3: 27 classes), 141 FP64 operations instead of 36 pairs x 8 Gauss points.
+    {
+        double* D1 = &s.x[el][0][0];
+        double* D2 = &s.xl[el][0][0];
+        double* D3 = &s.m[el][0];
+        if (valid)
+            for (int i = t; i < 12; i += 8) {
+                const int c = i >> 2, gyz = i & 3;
+                D1[i] = fma(s.det[el][4 + gyz], p.tm[1][c], s.det[el][gyz] * p.tm[0][c]);
+            }
+        __syncthreads();
+        if (valid)
+            for (int i = t; i < 18; i += 8) {
+                const int cx = i / 6, r = i - 6 * cx, cy = r >> 1, gz = r & 1;
+                D2[i] = fma(D1[cx * 4 + 2 + gz], p.tm[1][cy], D1[cx * 4 + gz] * p.tm[0][cy]);
+            }
+        __syncthreads();
+        if (valid)
+            for (int i = t; i < 27; i += 8) {
+                const int cxy = i / 3, cz = i - 3 * cxy;
+                D3[i] = p.DE * fma(D2[cxy * 2 + 1], p.tm[1][cz], D2[cxy * 2] * p.tm[0][cz]);
+            }
+        __syncthreads();
+    }
+
     // ---- phase B: node pairs -----------------------------------------------------------
     double* rec = p.rec + (valid ? e : 0) * kRec;
-    const double lam = p.lam, mu = p.mu, D0d = p.D0d, DE = p.DE;
+    const double lam = p.lam, mu = p.mu, D0d = p.D0d;
     // diagonal pair (t, t): P symmetric
     if (valid) {
         const int a = t, pi = pair_index(a, a);
-        double P00 = 0, P11 = 0, P22 = 0, P01 = 0, P02 = 0, P12 = 0, m = 0;
+        double P00 = 0, P11 = 0, P22 = 0, P01 = 0, P02 = 0, P12 = 0;
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const double r0 = s.R[el][g][3 * a], r1 = s.R[el][g][3 * a + 1], r2 = s.R[el][g][3 * a + 2];
@@ -197,7 +235,6 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
             P01 = fma(q0, r1, P01);
             P02 = fma(q0, r2, P02);
             P12 = fma(q1, r2, P12);
-            m = fma(s.det[el][g], s.nn[pi][g], m);
         }
         const double lm = lam + mu;
         double* o = rec + kPairStride * pi - 2 * a;  // pair_offset(a, a)
@@ -207,9 +244,8 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
         o[3] = lm * P01;
         o[4] = lm * P02;
         o[5] = lm * P12;
-        o[6] = DE * m;
+        o[6] = s.m[el][mass_class(a, a)];
         o[7] = 0.0;  // the unused slot: whole 32-byte sectors written, none read back from DRAM
-        s.m[el][pi] = o[6];
     }
     // off-diagonal pairs
     for (int q = t; q < 28 && valid; q += 8) {
@@ -217,7 +253,6 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
         offdiag_pair(q, a, b);
         const int pi = pair_index(a, b);
         double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        double m = 0;
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const double q0 = s.Rs[el][g][3 * a], q1 = s.Rs[el][g][3 * a + 1], q2 = s.Rs[el][g][3 * a + 2];
@@ -231,7 +266,6 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
             P[2][0] = fma(q2, r0, P[2][0]);
             P[2][1] = fma(q2, r1, P[2][1]);
             P[2][2] = fma(q2, r2, P[2][2]);
-            m = fma(s.det[el][g], s.nn[pi][g], m);
         }
         double* o = rec + kPairStride * pi - 2 * (a + 1);  // pair_offset(a, b), a < b
         o[0] = D0d * P[0][0] + mu * (P[1][1] + P[2][2]);
@@ -243,8 +277,7 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
         o[5] = lam * P[1][2] + mu * P[2][1];
         o[6] = lam * P[2][0] + mu * P[0][2];
         o[7] = lam * P[2][1] + mu * P[1][2];
-        o[9] = DE * m;
-        s.m[el][pi] = o[9];
+        o[9] = s.m[el][mass_class(a, b)];
     }
     // element load for corner t: F_t = sum_b M_tb W x_b (the mass blocks of the other threads'
     // pairs come through shared memory)
@@ -253,7 +286,7 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
         double f0 = 0, f1 = 0, f2 = 0;
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
-            const double mv = s.m[el][pair_index(min(t, b), max(t, b))];
+            const double mv = s.m[el][mass_class(t, b)];
             f0 = fma(mv, s.wx[el][b][0], f0);
             f1 = fma(mv, s.wx[el][b][1], f1);
             f2 = fma(mv, s.wx[el][b][2], f2);
@@ -735,10 +768,14 @@ int launch_hex8_element(const fem_mesh* mesh, const fem_material* mat, void* wor
             for (int j = 0; j < 3; ++j) ep.wc[i][j] = wc[i][j];
     }
     ep.tab = make_tables();
-    const ShapeTables& T = shape_tables();
-    for (int a = 0; a < 8; ++a)
-        for (int b = a; b < 8; ++b)
-            for (int g = 0; g < 8; ++g) ep.nn[pair_index(a, b)][g] = T.nr[g][a] * T.nr[g][b];
+    {
+        // 1D shape factors (1 + s x) / 2 at x = +-kGS1: al for a corner on the Gauss point's
+        // side, be for the other side
+        const double al = 0.5 * (1.0 + kGS1), be = 0.5 * (1.0 - kGS1);
+        const double tm[2][3] = {{al * al, al * be, be * be}, {be * be, al * be, al * al}};
+        for (int sd = 0; sd < 2; ++sd)
+            for (int c = 0; c < 3; ++c) ep.tm[sd][c] = tm[sd][c];
+    }
     const size_t smem = sizeof(ElemSmem);
     FEM_CUDA(cudaFuncSetAttribute(k_hex8_element, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t blocks = (e_end - e_begin + kEpc - 1) / kEpc;
