@@ -920,38 +920,55 @@ int assemble_host_impl(const fem_mesh* mesh, const fem_material* mat, const fem_
     cudaStream_t st = as_stream(stream);
     const bool dd = out->algo == FEM_ALGO_DD;
     const int parts = n_parts;
-    std::vector<cudaEvent_t> done(parts, nullptr), copied(parts, nullptr);
-    cudaStream_t cs = nullptr;
-    cudaEvent_t fin = nullptr;
+    std::vector<cudaEvent_t> elems(parts, nullptr), done(parts, nullptr), copied(parts, nullptr);
+    cudaStream_t cs = nullptr, gs = nullptr;
+    cudaEvent_t start = nullptr, fin = nullptr;
     auto cleanup = [&] {
-        for (cudaEvent_t e : done)
-            if (e) cudaEventDestroy(e);
-        for (cudaEvent_t e : copied)
-            if (e) cudaEventDestroy(e);
+        for (auto* v : {&elems, &done, &copied})
+            for (cudaEvent_t e : *v)
+                if (e) cudaEventDestroy(e);
+        if (start) cudaEventDestroy(start);
         if (fin) cudaEventDestroy(fin);
         if (cs) cudaStreamDestroy(cs);
+        if (gs) cudaStreamDestroy(gs);
     };
     auto fail = [&](cudaError_t e, const char* what) {
         cleanup();
         return cuda_status(e, what);
     };
-    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return fail(e, "cudaStreamCreateWithFlags");
-    // all kernels first (a copy into pageable memory may block the host until it ends)
+    int lo_prio = 0, hi_prio = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (e != cudaSuccess) return fail(e, "cudaDeviceGetStreamPriorityRange");
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, hi_prio)) != cudaSuccess)
+        return fail(e, "stream creation");
+    if ((e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventRecord(start, st)) != cudaSuccess || (e = cudaStreamWaitEvent(gs, start, 0)) != cudaSuccess)
+        return fail(e, "gather stream ordering");
+    // All kernels first (a copy into pageable memory may block the host until it ends).  The
+    // element parts run in order on the caller's stream and the gathers on a second,
+    // highest-priority stream, gather q after element part q: the gather of part q fills the
+    // partial last waves of element part q + 1 instead of waiting for them, and part q's copy
+    // can start as soon as its gather ends.  Records of different parts never overlap, so the
+    // results do not depend on how the two streams interleave.
     for (int q = 0; q < parts; ++q) {
-        if (dd) {
-            rc = launch_hex8_element_dd(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
-            if (!rc) rc = launch_gather_dd(mesh, out, workspace, st, row_split[q], row_split[q + 1]);
-        } else {
-            rc = launch_hex8_element(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
-            if (!rc) rc = launch_gather64(mesh, out, workspace, st, row_split[q], row_split[q + 1]);
+        rc = dd ? launch_hex8_element_dd(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1])
+                : launch_hex8_element(mesh, mat, workspace, st, elem_split[q], elem_split[q + 1]);
+        if (rc) {
+            cleanup();
+            return rc;
         }
+        if ((e = cudaEventCreateWithFlags(&elems[q], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventRecord(elems[q], st)) != cudaSuccess || (e = cudaStreamWaitEvent(gs, elems[q], 0)) != cudaSuccess)
+            return fail(e, "element part event");
+        rc = dd ? launch_gather_dd(mesh, out, workspace, gs, row_split[q], row_split[q + 1])
+                : launch_gather64(mesh, out, workspace, gs, row_split[q], row_split[q + 1]);
         if (rc) {
             cleanup();
             return rc;
         }
         if ((e = cudaEventCreateWithFlags(&done[q], cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventRecord(done[q], st)) != cudaSuccess)
+            (e = cudaEventRecord(done[q], gs)) != cudaSuccess)
             return fail(e, "cudaEventRecord");
     }
     const int64_t kq = 9, mq = out->m_layout == FEM_LAYOUT_BSR ? 1 : 3;
