@@ -449,6 +449,7 @@ struct Gather64Params {
     const int32_t* ne_ptr;
     const int32_t* ne_list;
     const uint8_t* slot_map;
+    int slot_map_aligned;  // slot_map on an 8-byte boundary: one 8-byte load per entry
     const int4* conn4;
     const double* rec;
     int k_layout, m_layout;
@@ -522,7 +523,7 @@ __device__ void gather_row_long64(const Gather64Params& p, int64_t row, int lane
     }
 }
 
-__global__ void __launch_bounds__(kG64Warps * 32) k_gather64(const Gather64Params p) {
+__global__ void __launch_bounds__(kG64Warps * 32, 6) k_gather64(const Gather64Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Gather64Smem& S = *reinterpret_cast<Gather64Smem*>(smem_raw);
     const unsigned full = 0xffffffffu;
@@ -537,19 +538,25 @@ __global__ void __launch_bounds__(kG64Warps * 32) k_gather64(const Gather64Param
     const int ks = vrow ? p.ne_ptr[row] : 0;
     const int cnt = vrow ? p.ne_ptr[row + 1] - ks : 0;
 
-    // ---- F of this row (lanes b < 3): corner loads in element order + nodal loads ----------
-    if (p.F && vrow && b < 3) {
-        double f = 0.0;
-        for (int k = 0; k < cnt; ++k) {
-            const int ent = __ldg(p.ne_list + ks + k);
-            f += __ldg(p.rec + int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b);
+    // F of this row on lanes b < 3 (corner loads in element order, then the nodal loads) for
+    // the warps that leave before the main path
+    auto row_F = [&]() {
+        if (p.F && vrow && b < 3) {
+            double f = 0.0;
+            for (int k = 0; k < cnt; ++k) {
+                const int ent = __ldg(p.ne_list + ks + k);
+                f += __ldg(p.rec + int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b);
+            }
+            if (p.loads) f += p.loads[3 * row + b];
+            p.F[3 * row + b] = f;
         }
-        if (p.loads) f += p.loads[3 * row + b];
-        p.F[3 * row + b] = f;
+    };
+    if (!p.K && !p.M) {
+        row_F();
+        return;
     }
-    if (!p.K && !p.M) return;
-
     if (__any_sync(full, L > kG64MaxL)) {
+        row_F();
         for (int rr = 0; rr < kG64Rows; ++rr)
             if (row0 + rr < p.row_end) gather_row_long64(p, row0 + rr, lane);
         return;
@@ -562,20 +569,63 @@ __global__ void __launch_bounds__(kG64Warps * 32) k_gather64(const Gather64Param
     int maxcnt = cnt;
 #pragma unroll
     for (int off = 8; off < 32; off <<= 1) maxcnt = max(maxcnt, __shfl_xor_sync(full, maxcnt, off));
+
+    // The row's incident entries, 8 at a time: lane (r, j) holds entry 8c + j of chunk c (its
+    // ne_list value and its 8 slot_map bytes), and every lane of the row takes entry k from
+    // lane (r, k mod 8) by a shuffle, so the element block loads of entry k + 1 issue without
+    // first waiting for a load of ne_list.
+    const int src = lane & ~7;
+    int ent_reg = 0;
+    unsigned long long sm_reg = 0ull;
+    auto load_chunk = [&](int c) {
+        const int j = 8 * c + b;
+        ent_reg = j < cnt ? __ldg(p.ne_list + ks + j) : 0;
+        if (j < cnt) {
+            if (p.slot_map_aligned) {
+                sm_reg = __ldg(reinterpret_cast<const unsigned long long*>(p.slot_map) + (ks + j));
+            } else {
+                sm_reg = 0ull;
+                for (int q = 0; q < 8; ++q)
+                    sm_reg |= (unsigned long long)__ldg(p.slot_map + 8 * int64_t(ks + j) + q) << (8 * q);
+            }
+        }
+    };
+    load_chunk(0);
+    // F of this row on lanes b < 3: corner loads in element order, then the nodal loads
+    if (p.F) {
+        double f = 0.0;
+        for (int k = 0; k < maxcnt; ++k) {
+            if (k > 0 && (k & 7) == 0) load_chunk(k >> 3);
+            const int ent = __shfl_sync(full, ent_reg, src | (k & 7));
+            if (b < 3 && k < cnt) f += __ldg(p.rec + int64_t(ent >> 3) * kRec + kFOff + 3 * (ent & 7) + b);
+        }
+        if (maxcnt > 8) load_chunk(0);
+        if (b < 3 && vrow) {
+            if (p.loads) f += p.loads[3 * row + b];
+            p.F[3 * row + b] = f;
+        }
+    }
     unsigned touched = 0;  // slots of row r holding a value (the same in the row's 8 lanes)
     double cur[kPairStride], nxt[kPairStride];
     int cur_slot = 0, nxt_slot = 0;
-    if (cnt > 0) {
-        const int ent = __ldg(p.ne_list + ks);
-        load_pair_block(p.rec, ent >> 3, ent & 7, b, cur);
-        cur_slot = __ldg(p.slot_map + 8 * int64_t(ks) + b);
+    if (maxcnt > 0) {
+        const int ent = __shfl_sync(full, ent_reg, src);
+        const unsigned long long wd = __shfl_sync(full, sm_reg, src);
+        if (cnt > 0) {
+            load_pair_block(p.rec, ent >> 3, ent & 7, b, cur);
+            cur_slot = int((wd >> (8 * b)) & 0xffull);
+        }
     }
     for (int k = 0; k < maxcnt; ++k) {
         const bool active = k < cnt;
-        if (k + 1 < cnt) {
-            const int ent = __ldg(p.ne_list + ks + k + 1);
-            load_pair_block(p.rec, ent >> 3, ent & 7, b, nxt);
-            nxt_slot = __ldg(p.slot_map + 8 * int64_t(ks + k + 1) + b);
+        if (k + 1 < maxcnt) {  // uniform over the warp
+            if (((k + 1) & 7) == 0) load_chunk((k + 1) >> 3);
+            const int ent = __shfl_sync(full, ent_reg, src | ((k + 1) & 7));
+            const unsigned long long wd = __shfl_sync(full, sm_reg, src | ((k + 1) & 7));
+            if (k + 1 < cnt) {
+                load_pair_block(p.rec, ent >> 3, ent & 7, b, nxt);
+                nxt_slot = int((wd >> (8 * b)) & 0xffull);
+            }
         }
         // a repeated corner node (degenerate element) maps two corners to one slot
         bool dup = false;
@@ -819,6 +869,7 @@ int launch_gather64(const fem_mesh* mesh, const fem_assembly_out* out, const voi
     gp.ne_ptr = mesh->ne_ptr;
     gp.ne_list = mesh->ne_list;
     gp.slot_map = mesh->slot_map;
+    gp.slot_map_aligned = (reinterpret_cast<uintptr_t>(mesh->slot_map) & 7) == 0;
     gp.conn4 = reinterpret_cast<const int4*>(mesh->conn);
     gp.rec = static_cast<const double*>(workspace);
     gp.k_layout = out->k_layout;
