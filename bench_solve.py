@@ -389,6 +389,7 @@ def c4_study(net=None, device="cuda", rtol=1e-10, train_kw=None, nrhs=32, smooth
     rows += compare(S, Urm, [("fp64_bj_32rhs", dict(rtol=rtol, mixed=False)),
                              ("mixed_bj_32rhs", dict(rtol=rtol, mixed=True)),
                              ("mixed_learned_32rhs", dict(rtol=rtol, mixed=True, precond=Pl)),
+                             ("mixed_amg_32rhs", dict(rtol=rtol, mixed=True, precond="amg")),
                              ("fp64_amg_32rhs", dict(rtol=rtol, mixed=False, precond="amg"))], F=Fm, amg=amg)
     # learned smoother weights (trained on the same family) in a second hierarchy of K
     sm_info = {}

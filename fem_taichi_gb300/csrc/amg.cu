@@ -407,6 +407,12 @@ unsigned grid_for(int64_t work_items, int per_cta) {
     return unsigned(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sm_count()) * 8)));
 }
 
+// Grid of a grid-stride block-row product: one wave of resident CTAs (a second, partial wave
+// would run with too few warps to hide the gathers' latency).
+unsigned product_grid(const void* kernel, int64_t rows, int rows_per_cta) {
+    return resident_grid(kernel, kThreads, (rows + rows_per_cta - 1) / rows_per_cta, int64_t(sm_count()) * 8);
+}
+
 int lanes_for(const DevBsr& M) {
     const double avg = M.n > 0 ? double(M.nnzb) / double(M.n) : 1.0;
     return avg < 6 ? 4 : avg < 16 ? 8 : avg < 48 ? 16 : 32;
@@ -446,23 +452,27 @@ int launch_gen(const DevBsr& M, const float* x, const Epi& epi, const PcgState* 
         FEM_LAUNCH_CHECK("amg block-row product (split rows)");
         return FEM_OK;
     }
+    auto run = [&](auto kernel, int rows_per_cta) {
+        kernel<<<product_grid(reinterpret_cast<const void*>(kernel), M.n, rows_per_cta), kThreads, 0, s>>>(v, x, epi,
+                                                                                                             st);
+    };
     if (R == 1) {
         const int lpr = lanes_for(M);
-        const unsigned g = grid_for(M.n, (kThreads / 32) * (32 / lpr));
+        const int rpc = (kThreads / 32) * (32 / lpr);
         switch (lpr) {
-            case 4: k_bsrg1<BR, BC, 4><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            case 8: k_bsrg1<BR, BC, 8><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            case 16: k_bsrg1<BR, BC, 16><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            default: k_bsrg1<BR, BC, 32><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
+            case 4: run(k_bsrg1<BR, BC, 4, Epi>, rpc); break;
+            case 8: run(k_bsrg1<BR, BC, 8, Epi>, rpc); break;
+            case 16: run(k_bsrg1<BR, BC, 16, Epi>, rpc); break;
+            default: run(k_bsrg1<BR, BC, 32, Epi>, rpc); break;
         }
     } else {
-        const unsigned g = grid_for(M.n, (kThreads / 32) * (32 / R));
+        const int rpc = (kThreads / 32) * (32 / R);
         switch (R) {
-            case 2: k_bsrgR<BR, BC, 2><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            case 4: k_bsrgR<BR, BC, 4><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            case 8: k_bsrgR<BR, BC, 8><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            case 16: k_bsrgR<BR, BC, 16><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
-            default: k_bsrgR<BR, BC, 32><<<g, kThreads, 0, s>>>(v, x, epi, st); break;
+            case 2: run(k_bsrgR<BR, BC, 2, Epi>, rpc); break;
+            case 4: run(k_bsrgR<BR, BC, 4, Epi>, rpc); break;
+            case 8: run(k_bsrgR<BR, BC, 8, Epi>, rpc); break;
+            case 16: run(k_bsrgR<BR, BC, 16, Epi>, rpc); break;
+            default: run(k_bsrgR<BR, BC, 32, Epi>, rpc); break;
         }
     }
     FEM_LAUNCH_CHECK("amg block-row product");
@@ -471,17 +481,20 @@ int launch_gen(const DevBsr& M, const float* x, const Epi& epi, const PcgState* 
 
 template <typename Epi>
 int launch_l0(const BsrView<float>& A, const float* x, const Epi& epi, const PcgState* st, int R, cudaStream_t s) {
+    auto run = [&](auto kernel, int rows_per_cta) {
+        kernel<<<product_grid(reinterpret_cast<const void*>(kernel), A.n, rows_per_cta), kThreads, 0, s>>>(A, x, epi,
+                                                                                                             st);
+    };
     if (R == 1) {
-        const unsigned g = grid_for(A.n, (kThreads / 32) * 4);
-        k_l0_1<8><<<g, kThreads, 0, s>>>(A, x, epi, st);
+        run(k_l0_1<8, Epi>, (kThreads / 32) * 4);
     } else {
-        const unsigned g = grid_for(A.n, (kThreads / 32) * (32 / R));
+        const int rpc = (kThreads / 32) * (32 / R);
         switch (R) {
-            case 2: k_l0_R<2><<<g, kThreads, 0, s>>>(A, x, epi, st); break;
-            case 4: k_l0_R<4><<<g, kThreads, 0, s>>>(A, x, epi, st); break;
-            case 8: k_l0_R<8><<<g, kThreads, 0, s>>>(A, x, epi, st); break;
-            case 16: k_l0_R<16><<<g, kThreads, 0, s>>>(A, x, epi, st); break;
-            default: k_l0_R<32><<<g, kThreads, 0, s>>>(A, x, epi, st); break;
+            case 2: run(k_l0_R<2, Epi>, rpc); break;
+            case 4: run(k_l0_R<4, Epi>, rpc); break;
+            case 8: run(k_l0_R<8, Epi>, rpc); break;
+            case 16: run(k_l0_R<16, Epi>, rpc); break;
+            default: run(k_l0_R<32, Epi>, rpc); break;
         }
     }
     FEM_LAUNCH_CHECK("amg level-0 product");

@@ -511,39 +511,37 @@ Layout layout(int64_t n, int R, int mixed) {
     return L;
 }
 
-unsigned vec_grid(int64_t work) {
-    const int64_t need = (work + kThreads - 1) / kThreads;
-    return unsigned(std::max<int64_t>(1, std::min<int64_t>(need, std::min<int64_t>(kMaxCtas, int64_t(sm_count()) * 2))));
+// Grid of a grid-stride vector kernel over `work` items: one wave of resident CTAs (these
+// kernels stream HBM and need every warp slot to keep enough loads in flight), at most
+// kMaxCtas (the partial-sum buffer of their dot products).
+template <typename Kernel>
+unsigned vec_grid(Kernel kernel, int64_t work) {
+    return resident_grid(reinterpret_cast<const void*>(kernel), kThreads, (work + kThreads - 1) / kThreads, kMaxCtas);
 }
 
-template <typename T>
-unsigned spmv_grid(int64_t n, int R, int variant) {
-    int64_t rows_per_cta, cap;
-    if (R == 1) {
-        const SpmvVariant v = spmv_variant(variant);
-        rows_per_cta = int64_t(kThreads / 32) * (32 / v.lpr);
-        cap = int64_t(sm_count()) * (v.ctas_per_sm * v.threads / kThreads);
-    } else {
-        rows_per_cta = int64_t(kThreads / 32) * (32 / R);
-        cap = int64_t(sm_count()) * 8;
-    }
-    const int64_t need = (n + rows_per_cta - 1) / rows_per_cta;
-    return unsigned(std::max<int64_t>(1, std::min<int64_t>({need, cap, int64_t(kMaxCtas)})));
-}
-
+// Grid of the product kernel: one wave of resident CTAs (grid-stride rows), at most kMaxCtas
+// (the size of the partial-sum buffer).  The grid fixes each row's CTA, hence the order of the
+// dot-product partial sums.
 template <typename T, int R>
 void launch_spmv_pq(const BsrView<T>& A, const T* p, T* q, double* part, PcgState* st, int variant, cudaStream_t s) {
-    const unsigned g = spmv_grid<T>(A.n, R, variant);
+    auto run = [&](auto kernel, int64_t rows_per_cta, int64_t cap, int r) {
+        const unsigned g = resident_grid(reinterpret_cast<const void*>(kernel), kThreads,
+                                         (A.n + rows_per_cta - 1) / rows_per_cta, std::min<int64_t>(cap, kMaxCtas));
+        kernel<<<g, kThreads, 0, s>>>(A, p, q, part, st, r);
+    };
     if (R > 1) {
-        k_spmv_pq<T, R><<<g, kThreads, 0, s>>>(A, p, q, part, st, R);
+        run(k_spmv_pq<T, R>, int64_t(kThreads / 32) * (32 / R), int64_t(sm_count()) * 8, R);
         return;
     }
-    switch (spmv_variant(variant).lpr) {
-        case 32: k_spmv_pq<T, 32><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
-        case 16: k_spmv_pq<T, 16><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
-        case 8: k_spmv_pq<T, 8><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
-        case 4: k_spmv_pq<T, 4><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
-        default: k_spmv_pq<T, 2><<<g, kThreads, 0, s>>>(A, p, q, part, st, 1); break;
+    const SpmvVariant v = spmv_variant(variant);
+    const int64_t rows_per_cta = int64_t(kThreads / 32) * (32 / v.lpr);
+    const int64_t cap = int64_t(sm_count()) * (v.ctas_per_sm * v.threads / kThreads);
+    switch (v.lpr) {
+        case 32: run(k_spmv_pq<T, 32>, rows_per_cta, cap, 1); break;
+        case 16: run(k_spmv_pq<T, 16>, rows_per_cta, cap, 1); break;
+        case 8: run(k_spmv_pq<T, 8>, rows_per_cta, cap, 1); break;
+        case 4: run(k_spmv_pq<T, 4>, rows_per_cta, cap, 1); break;
+        default: run(k_spmv_pq<T, 2>, rows_per_cta, cap, 1); break;
     }
 }
 
@@ -551,11 +549,10 @@ template <typename T, int R>
 int launch_iterations(const BsrView<T>& A, const T* M, T* x, T* r, T* z, T* p, T* q, double* part, PcgState* st,
                       int variant, int count, cudaStream_t s) {
     const int64_t nv = 3 * A.n * R;
-    const unsigned gv = vec_grid(nv), gn = vec_grid(A.n * R);
     for (int i = 0; i < count; ++i) {
-        k_p_update<T, R><<<gv, kThreads, 0, s>>>(nv, z, p, st);
+        k_p_update<T, R><<<vec_grid(k_p_update<T, R>, nv), kThreads, 0, s>>>(nv, z, p, st);
         launch_spmv_pq<T, R>(A, p, q, part, st, variant, s);
-        k_update<T, R><<<gn, kThreads, 0, s>>>(A.n, M, p, q, x, r, z, part, st);
+        k_update<T, R><<<vec_grid(k_update<T, R>, A.n * R), kThreads, 0, s>>>(A.n, M, p, q, x, r, z, part, st);
     }
     FEM_LAUNCH_CHECK("pcg iteration");
     return FEM_OK;
@@ -632,7 +629,7 @@ int pcg_core(const BsrView<T>& A, const T* M, const T* b, T* x, T* r, T* z, T* p
              double rtol, int maxit, int variant, int use_graph, int unroll, cudaStream_t s, InnerResult* res,
              int stall = 0) {
     auto init = [&](cudaStream_t ss) -> int {
-        k_init<T, R><<<vec_grid(A.n * R), kThreads, 0, ss>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
+        k_init<T, R><<<vec_grid(k_init<T, R>, A.n * R), kThreads, 0, ss>>>(A.n, M, b, x, r, z, part, st, rtol, maxit);
         FEM_LAUNCH_CHECK("k_init");
         return FEM_OK;
     };
@@ -650,7 +647,6 @@ int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, c
                  T* q, double* part, PcgState* st, double rtol, int maxit, int variant, int use_graph, int unroll,
                  cudaStream_t s, InnerResult* res, int stall = 0) {
     const int64_t nv = 3 * A.n * R;
-    const unsigned gv = vec_grid(nv);
     constexpr bool f64 = sizeof(T) == 8;
     float* r32 = f64 ? amg->r32 : nullptr;
     float* z32 = f64 ? amg->z32 : nullptr;
@@ -658,22 +654,22 @@ int pcg_core_amg(const BsrView<T>& A, const BsrView<float>& A32, fem_amg* amg, c
     float* zout = f64 ? z32 : reinterpret_cast<float*>(z);
     const T* qflex = f64 ? q : nullptr;
     auto init = [&](cudaStream_t ss) -> int {
-        k_init_r<T, R><<<gv, kThreads, 0, ss>>>(nv, b, x, r, r32, part, st, rtol, maxit);
+        k_init_r<T, R><<<vec_grid(k_init_r<T, R>, nv), kThreads, 0, ss>>>(nv, b, x, r, r32, part, st, rtol, maxit);
         FEM_LAUNCH_CHECK("k_init_r");
         int rc = amg::vcycle(amg, A32, rin, zout, st, R, f64, ss);
         if (rc) return rc;
-        k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, nullptr, part, st);
+        k_rz<T, R><<<vec_grid(k_rz<T, R>, nv), kThreads, 0, ss>>>(nv, r, z, z32, nullptr, part, st);
         FEM_LAUNCH_CHECK("k_rz");
         return FEM_OK;
     };
     auto iters = [&](int count, cudaStream_t ss) -> int {
         for (int i = 0; i < count; ++i) {
-            k_p_update<T, R><<<gv, kThreads, 0, ss>>>(nv, z, p, st);
+            k_p_update<T, R><<<vec_grid(k_p_update<T, R>, nv), kThreads, 0, ss>>>(nv, z, p, st);
             launch_spmv_pq<T, R>(A, p, q, part, st, variant, ss);
-            k_update_r<T, R><<<gv, kThreads, 0, ss>>>(nv, p, q, x, r, r32, part, st);
+            k_update_r<T, R><<<vec_grid(k_update_r<T, R>, nv), kThreads, 0, ss>>>(nv, p, q, x, r, r32, part, st);
             int rc = amg::vcycle(amg, A32, rin, zout, st, R, f64, ss);
             if (rc) return rc;
-            k_rz<T, R><<<gv, kThreads, 0, ss>>>(nv, r, z, z32, qflex, part, st);
+            k_rz<T, R><<<vec_grid(k_rz<T, R>, nv), kThreads, 0, ss>>>(nv, r, z, z32, qflex, part, st);
         }
         FEM_LAUNCH_CHECK("pcg iteration (amg)");
         return FEM_OK;
@@ -699,9 +695,9 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
     // r = F - K u (FP64 or compensated), its norms and rounding scales -> h
     auto true_residual = [&](const double* u, double* r) -> int {
         if (extra)
-            k_residual_ex<R, true><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
+            k_residual_ex<R, true><<<vec_grid(k_residual_ex<R, true>, nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
         else
-            k_residual_ex<R, false><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
+            k_residual_ex<R, false><<<vec_grid(k_residual_ex<R, false>, nv), kThreads, 0, s>>>(K64, F, u, r, part, st);
         FEM_LAUNCH_CHECK("k_residual_ex");
         FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
         FEM_CUDA(cudaStreamSynchronize(s));
@@ -714,9 +710,9 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
         // ||F_k||: the residual of u = 0
         double* z0 = reinterpret_cast<double*>(ws + L.v64[0]);
         double* r0 = reinterpret_cast<double*>(ws + L.v64[1]);
-        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, z0);
+        k_zero<<<vec_grid(k_zero, nv), kThreads, 0, s>>>(nv, z0);
         FEM_LAUNCH_CHECK("k_zero");
-        k_residual_ex<R, false><<<vec_grid(nv), kThreads, 0, s>>>(K64, F, z0, r0, part, st);
+        k_residual_ex<R, false><<<vec_grid(k_residual_ex<R, false>, nv), kThreads, 0, s>>>(K64, F, z0, r0, part, st);
         FEM_LAUNCH_CHECK("k_residual_ex");
         FEM_CUDA(cudaMemcpyAsync(&h, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
         FEM_CUDA(cudaStreamSynchronize(s));
@@ -778,7 +774,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
                 if (sc[k] > 0) tol = std::min(tol, o->rtol * bnorm[k] / sc[k]);
             tol = std::max(tol, 1e-15);
             FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
-            k_mask_rhs<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, scale, rt);
+            k_mask_rhs<R><<<vec_grid(k_mask_rhs<R>, nv), kThreads, 0, s>>>(nv, scale, rt);
             FEM_LAUNCH_CHECK("k_mask_rhs");
             if ((rc = core(rt, d, tol, maxit - total_iters))) return rc;
             total_iters += ir.iters;
@@ -787,7 +783,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
                 status = ir.status;
                 break;
             }
-            k_add<<<vec_grid(nv), kThreads, 0, s>>>(nv, d, U);
+            k_add<<<vec_grid(k_add, nv), kThreads, 0, s>>>(nv, d, U);
             FEM_LAUNCH_CHECK("k_add");
             if ((rc = true_residual(U, rt))) return rc;
             const double w = worst_rel();
@@ -807,7 +803,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
         float* M32 = reinterpret_cast<float*>(ws + L.m32);
         int rc = amg ? FEM_OK : fem_convert_f64_to_f32(M64, M32, 9 * n, s);
         if (rc) return rc;
-        k_zero<<<vec_grid(nv), kThreads, 0, s>>>(nv, U);
+        k_zero<<<vec_grid(k_zero, nv), kThreads, 0, s>>>(nv, U);
         FEM_LAUNCH_CHECK("k_zero");
         rc = true_residual(U, r64);
         if (rc) return rc;
@@ -819,7 +815,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
             if (outer > 0 && !(worst < 0.5 * prev)) break;  // refinement stalled
             prev = worst;
             FEM_CUDA(cudaMemcpyAsync(scale, sc, sizeof(double) * R, cudaMemcpyHostToDevice, s));
-            k_scale_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, r64, scale, b32);
+            k_scale_cast<R><<<vec_grid(k_scale_cast<R>, nv), kThreads, 0, s>>>(nv, r64, scale, b32);
             FEM_LAUNCH_CHECK("k_scale_cast");
             if (amg)
                 rc = pcg_core_amg<float, R>(K32, K32, amg, b32, d32, rr, zz, pp, qq, part, st, o->inner_rtol,
@@ -839,7 +835,7 @@ int solve_r(const fem_bsr* A64, const fem_bsr* A32, const double* M64, fem_amg* 
                 status = ir.status;
                 break;
             }
-            k_axpy_cast<R><<<vec_grid(nv), kThreads, 0, s>>>(nv, scale, d32, U);
+            k_axpy_cast<R><<<vec_grid(k_axpy_cast<R>, nv), kThreads, 0, s>>>(nv, scale, d32, U);
             FEM_LAUNCH_CHECK("k_axpy_cast");
             rc = true_residual(U, r64);
             if (rc) return rc;

@@ -1,7 +1,9 @@
 // BSR SpMV / SpMM entry points, precision conversion, block-Jacobi inverse and the SpMV
 // launch autotuner.  The kernels are the residual product of SOLVE_static.py:36 (K * U)
 // generalised to FP32 and to many right-hand sides.
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "spmv.cuh"
 
@@ -12,6 +14,38 @@ int sm_count() {
     if (cudaGetDevice(&dev) != cudaSuccess) return 148;
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
     return n;
+}
+
+int resident_ctas(const void* kernel, int threads, size_t smem) {
+    struct Entry {
+        const void* kernel;
+        int threads;
+        size_t smem;
+        int dev;
+        int ctas;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        for (const Entry& e : cache)
+            if (e.kernel == kernel && e.threads == threads && e.smem == smem && e.dev == dev) return e.ctas;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    cache.push_back({kernel, threads, smem, dev, n});
+    return n;
+}
+
+unsigned resident_grid(const void* kernel, int threads, int64_t need, int64_t cap) {
+    const int64_t wave = int64_t(sm_count()) * resident_ctas(kernel, threads, 0);
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>({need, wave, cap})));
 }
 
 namespace {
@@ -114,29 +148,34 @@ __global__ void k_block_jacobi(int64_t n, const int32_t* __restrict__ indptr, co
 
 template <typename T>
 int launch_spmv(const BsrView<T>& A, int nrhs, const T* x, T* y, int variant, cudaStream_t st) {
+    // Grid-stride kernels: one wave of resident CTAs (a grid larger than what fits leaves a
+    // second, partial wave with too few warps to keep the pipes busy)
     const int sms = sm_count();
+    auto run = [&](auto kernel, int threads, int64_t rows_per_cta, int64_t cap) {
+        const unsigned grid = resident_grid(reinterpret_cast<const void*>(kernel), threads,
+                                            (A.n + rows_per_cta - 1) / rows_per_cta, cap);
+        kernel<<<grid, threads, 0, st>>>(A, x, y);
+    };
     if (nrhs == 1) {
         const SpmvVariant v = spmv_variant(variant);
         const int64_t rows_per_cta = int64_t(v.threads / 32) * (32 / v.lpr);
-        const int64_t need = (A.n + rows_per_cta - 1) / rows_per_cta;
-        const unsigned grid = unsigned(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * v.ctas_per_sm)));
+        const int64_t cap = int64_t(sms) * v.ctas_per_sm;
         switch (v.lpr) {
-            case 32: k_spmv<T, 32><<<grid, v.threads, 0, st>>>(A, x, y); break;
-            case 16: k_spmv<T, 16><<<grid, v.threads, 0, st>>>(A, x, y); break;
-            case 8: k_spmv<T, 8><<<grid, v.threads, 0, st>>>(A, x, y); break;
-            case 4: k_spmv<T, 4><<<grid, v.threads, 0, st>>>(A, x, y); break;
-            default: k_spmv<T, 2><<<grid, v.threads, 0, st>>>(A, x, y); break;
+            case 32: run(k_spmv<T, 32>, v.threads, rows_per_cta, cap); break;
+            case 16: run(k_spmv<T, 16>, v.threads, rows_per_cta, cap); break;
+            case 8: run(k_spmv<T, 8>, v.threads, rows_per_cta, cap); break;
+            case 4: run(k_spmv<T, 4>, v.threads, rows_per_cta, cap); break;
+            default: run(k_spmv<T, 2>, v.threads, rows_per_cta, cap); break;
         }
     } else {
         const int64_t rows_per_cta = 8 * (32 / nrhs);
-        const int64_t need = (A.n + rows_per_cta - 1) / rows_per_cta;
-        const unsigned grid = unsigned(std::max<int64_t>(1, std::min<int64_t>(need, int64_t(sms) * 8)));
+        const int64_t cap = int64_t(sms) * 8;
         switch (nrhs) {
-            case 2: k_spmm<T, 2><<<grid, 256, 0, st>>>(A, x, y); break;
-            case 4: k_spmm<T, 4><<<grid, 256, 0, st>>>(A, x, y); break;
-            case 8: k_spmm<T, 8><<<grid, 256, 0, st>>>(A, x, y); break;
-            case 16: k_spmm<T, 16><<<grid, 256, 0, st>>>(A, x, y); break;
-            default: k_spmm<T, 32><<<grid, 256, 0, st>>>(A, x, y); break;
+            case 2: run(k_spmm<T, 2>, 256, rows_per_cta, cap); break;
+            case 4: run(k_spmm<T, 4>, 256, rows_per_cta, cap); break;
+            case 8: run(k_spmm<T, 8>, 256, rows_per_cta, cap); break;
+            case 16: run(k_spmm<T, 16>, 256, rows_per_cta, cap); break;
+            default: run(k_spmm<T, 32>, 256, rows_per_cta, cap); break;
         }
     }
     FEM_LAUNCH_CHECK("bsr spmv");

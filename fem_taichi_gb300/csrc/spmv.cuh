@@ -290,5 +290,10 @@ __host__ __device__ inline SpmvVariant spmv_variant(int id) {
 }
 
 int sm_count();
+// CTAs of `kernel` resident on one SM with `threads` threads and `smem` bytes of dynamic shared
+// memory (occupancy query, cached per kernel, CTA shape and device).
+int resident_ctas(const void* kernel, int threads, size_t smem);
+// Grid for a grid-stride kernel: min(need, cap, one wave of resident CTAs on every SM).
+unsigned resident_grid(const void* kernel, int threads, int64_t need, int64_t cap);
 
 }  // namespace fem
