@@ -137,6 +137,40 @@ def test_degenerate_element_with_repeated_corner():
         assert_vec_close(M.Get_MatrixM().data, OM.Get_MatrixM().data)
 
 
+def test_many_incident_entries_and_unaligned_slot_map():
+    """Nodes with more than 8 incident (element, corner) entries -- every element listed twice,
+    so interior nodes have 16 -- take the FP64 gather's later chunks of 8 entries; both
+    arithmetic variants against the oracle.  A slot_map that does not start on an 8-byte
+    boundary (an offset view a C-ABI caller may pass) takes the byte-wise loads and gives the
+    same K, M, F bit for bit, on the device and through the host pipeline."""
+    P1 = F.hex_block(5, 4, 3, jitter=0.1, seed=11, fix="zmin")
+    P = F.Physics(P1.Node[0], P1.xyz, np.concatenate([P1.conn, P1.conn]).T, P1.Bounds, [])
+    assert np.diff(np.asarray(P.ne_ptr)).max() > 8
+    OM = O.OracleModel(P, STEEL, (0, 0, 100))
+    for algo in ALGOS:
+        M = F.Model("dup", P, STEEL, algo=algo)
+        assert_K_close(M.Get_MatrixKL(), OM.Get_MatrixKL())
+        assert_vec_close(M.Get_MatrixM().data, OM.Get_MatrixM().data)
+        assert_vec_close(M.Get_VectorF(), OM.Get_VectorF())
+    M = F.Model("dup", P, STEEL, algo="fp64")
+    Kd, Md, Fd = M.assemble(k_layout="csr", m_layout="csr")
+    Kh, Mh, Fh = M.assemble_host(3)
+    sm = M.mesh.slot_map
+    buf = torch.zeros(sm.numel() + 16, dtype=torch.uint8, device=sm.device)
+    buf[3:3 + sm.numel()].copy_(sm)
+    saved = M.mesh.c.slot_map
+    M.mesh.c.slot_map = buf.data_ptr() + 3
+    try:
+        Ku, Mu, Fu = M.assemble(k_layout="csr", m_layout="csr")
+        Khu, Mhu, Fhu = M.assemble_host(3)
+    finally:
+        M.mesh.c.slot_map = saved
+    torch.cuda.synchronize()
+    assert torch.equal(Ku, Kd) and torch.equal(Mu, Md) and torch.equal(Fu, Fd)
+    assert np.array_equal(Khu, Kh) and np.array_equal(Mhu, Mh) and np.array_equal(Fhu, Fh)
+    assert np.array_equal(Kh, Kd.cpu().numpy())
+
+
 @pytest.mark.parametrize("algo", ALGOS)
 def test_full_size_c2_against_c_oracle(algo, c2_oracle):
     """200x200x24 (960,000 elements): the whole BSR K, M and F against the threaded C
