@@ -13,8 +13,9 @@
 //     212-223) and writes it to the per-element workspace.
 //  2. k_stress_node -- one thread per node: sums its incident (element, corner) values in
 //     ascending element order (no atomics), divides by the element count (get_NdAve,
-//     :183-187), then computes the principal stresses with cyclic Jacobi rotations
-//     (descending order) and the reference's "VM" formula as written (:93-94).
+//     :183-187; one reciprocal, six products; an isolated node stays 0 * inf = NaN), then
+//     computes the principal stresses with cyclic Jacobi rotations (descending order) and the
+//     reference's "VM" formula as written (:93-94).
 #include <mutex>
 
 #include "fem_common.cuh"
@@ -160,8 +161,11 @@ __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams 
 // Eigenvalues of the symmetric 3x3 [[a00,a01,a02],[a01,a11,a12],[a02,a12,a22]] by cyclic
 // Jacobi rotations in Rutishauser's form (the rotated off-diagonal set to zero, the diagonal
 // updated as a_pp - t a_pq and a_qq + t a_pq, the third row rotated with tau = s / (1 + c);
-// Numerical Recipes, "jacobi"), off-diagonals negligible against both diagonals dropped after
-// four sweeps; capped at 32 sweeps; returned descending.
+// Numerical Recipes, "jacobi"); from the second sweep on, an off-diagonal below the last bit of
+// both diagonals (100 |a_pq| lost in |a_pp| and |a_qq|) is dropped instead of rotated -- its
+// rotation would move the diagonal by about a_pq^2 / (a_qq - a_pp) -- which ends a 3 x 3 in
+// about three sweeps instead of five; c = rsqrt(1 + t^2); capped at 32 sweeps; returned
+// descending.
 __device__ void sym3_eig_desc(double a00, double a11, double a22, double a01, double a12, double a02,
                               double& p1, double& p2, double& p3) {
     double d[3] = {a00, a11, a22};
@@ -177,7 +181,7 @@ __device__ void sym3_eig_desc(double a00, double a11, double a22, double a01, do
             double& aqr = pq == 0 ? o12 : pq == 1 ? o12 : o02;   // (q, r)
             if (apq == 0.0) continue;
             const double g = 100.0 * fabs(apq);
-            if (sweep > 3 && fabs(d[p]) + g == fabs(d[p]) && fabs(d[q]) + g == fabs(d[q])) {
+            if (sweep > 0 && fabs(d[p]) + g == fabs(d[p]) && fabs(d[q]) + g == fabs(d[q])) {
                 apq = 0.0;
                 continue;
             }
@@ -190,7 +194,7 @@ __device__ void sym3_eig_desc(double a00, double a11, double a22, double a01, do
                 t = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
                 if (theta < 0.0) t = -t;
             }
-            const double c = 1.0 / sqrt(1.0 + t * t), sn = t * c, tau = sn / (1.0 + c);
+            const double c = rsqrt(fma(t, t, 1.0)), sn = t * c, tau = sn / (1.0 + c);
             const double ht = t * apq;
             d[p] -= ht;
             d[q] += ht;
@@ -223,9 +227,9 @@ __global__ void __launch_bounds__(256) k_stress_node(int64_t n_node, const int32
 #pragma unroll
         for (int c = 0; c < 6; ++c) v[c] += __ldg(r + c);
     }
-    const double ce = double(co_elem[i]);
+    const double rce = 1.0 / double(co_elem[i]);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) v[c] = v[c] / ce;
+    for (int c = 0; c < 6; ++c) v[c] *= rce;
     double p1, p2, p3;
     // vector order [xx, yy, zz, xy, yz, xz] (POST_process.py:79-86)
     sym3_eig_desc(v[0], v[1], v[2], v[3], v[4], v[5], p1, p2, p3);
