@@ -59,8 +59,9 @@ ELEM_FP64_INSTR = (8 * 12 + 24 * 8 + 8 * (27 + 18 + 3 + 5 + 72 + 24) + 8 * (48 +
 # FP64 operations of one element of the stress element kernel (k_stress_element): corner 0
 # subtracted 48; trilinear coefficients of x and u 24 x 2 x (7 FMA + 1); per Gauss point J
 # and the displacement gradient 2 x 27 FMA, adjugate 27, det 5, reciprocal ~10, H 9 x 6,
-# stresses 18; extrapolation to the 8 corners 8 x 6 x 8 FMA.
-STRESS_ELEM_FP64_FLOPS = 48 + 24 * 2 * 15 + 8 * (2 * 54 + 27 + 5 + 10 + 54 + 18) + 2 * 8 * 6 * 8
+# stresses 18; extrapolation to the corners 6 x 8 FMA for each distinct row of the table (2 for
+# the reference's aliased GMat, the default).
+STRESS_ELEM_FP64_FLOPS = 48 + 24 * 2 * 15 + 8 * (2 * 54 + 27 + 5 + 10 + 54 + 18) + 2 * 2 * 6 * 8
 
 
 def parse():

@@ -8,14 +8,16 @@
 //     gradient at Gauss point g as H = (sum_a u_a (x) dN_a/dxi) . adj(J) / det, and the
 //     stresses  sigma_n = D0 (H00, H11, H22),  sigma_s = mu (H01+H10, H12+H21, H02+H20)
 //     (components xy, yz, xz as UnitVectorS orders them, POST_process.py:190-209).
-//     Thread j then forms corner j's extrapolated value sum_k W[j][k] sigma(k) with the
-//     caller's 8x8 weight table (get_NdSol / shapefunc_GS, POST_process.py:172-181,
-//     212-223) and writes it to the per-element workspace.
+//     Corner j's extrapolated value is sum_k W[j][k] sigma(k) with the caller's 8x8 weight
+//     table (get_NdSol / shapefunc_GS, POST_process.py:172-181, 212-223); the dot products of
+//     the table's distinct rows are spread over the element's threads, and thread j writes
+//     corner j's values to the per-element workspace.
 //  2. k_stress_node -- one thread per node: sums its incident (element, corner) values in
 //     ascending element order (no atomics), divides by the element count (get_NdAve,
 //     :183-187; one reciprocal, six products; an isolated node stays 0 * inf = NaN), then
 //     computes the principal stresses with cyclic Jacobi rotations (descending order) and the
 //     reference's "VM" formula as written (:93-94).
+#include <cstring>
 #include <mutex>
 
 #include "fem_common.cuh"
@@ -35,11 +37,14 @@ struct StressParams {
     int64_t n_elem;
     double* rec;  // [n_elem][8][6]
     double D0d, lam, mu;
-    double W[8][8];
+    double W[8][8];  // the distinct rows of the caller's extrapolation table
+    int nrow;        // how many
+    int row_of[8];   // corner j -> its row of W
 };
 
 struct StressSmem {
     double W[8][8];
+    double res[kEpc][8][6];  // extrapolated values of each distinct table row
     double x[kEpc][8][3];
     double u[kEpc][8][3];
     double cx[kEpc][8][3];  // trilinear coefficients of the element-local coordinates
@@ -146,16 +151,25 @@ __global__ void __launch_bounds__(kThreads) k_stress_element(const StressParams 
         s.sv[el][g][5] = mu * (H[0][2] + H[2][0]);
     }
     __syncthreads();
+    // Extrapolation: the table's distinct rows only (the reference's aliased GMat gives every
+    // even corner one row and every odd corner another: 12 dot products per element instead of
+    // 48), spread over the element's 8 threads; corner j then takes its row's values.
+    if (valid) {
+        const int nout = p.nrow * 6;
+        for (int o = t; o < nout; o += 8) {
+            const int r = o / 6, c = o - 6 * r;
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc = fma(s.W[r][k], s.sv[el][k][c], acc);
+            s.res[el][r][c] = acc;
+        }
+    }
+    __syncthreads();
     if (!valid) return;
-    const int j = t;
+    const int j = t, r = p.row_of[j];
     double* o = p.rec + (e * 8 + j) * 6;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        double acc = 0.0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) acc = fma(s.W[j][k], s.sv[el][k][c], acc);
-        o[c] = acc;
-    }
+    for (int c = 0; c < 6; ++c) o[c] = s.res[el][r][c];
 }
 
 // Eigenvalues of the symmetric 3x3 [[a00,a01,a02],[a01,a11,a12],[a02,a12,a22]] by cyclic
@@ -285,8 +299,18 @@ extern "C" int fem_stress_ex(const fem_mesh* mesh, const fem_material* mat, cons
         sp.D0d = EX * (1 - PO) / (1 + PO) / (1 - 2 * PO);  // POST_process.py:292-302
         sp.lam = EX * PO / (1 + PO) / (1 - 2 * PO);
         sp.mu = EX / 2 / (1 + PO);                          // :304-306
-        for (int j = 0; j < 8; ++j)
-            for (int k = 0; k < 8; ++k) sp.W[j][k] = extrap[8 * j + k];
+        // distinct rows of the table (exactly equal rows share one)
+        std::memset(sp.W, 0, sizeof(sp.W));
+        sp.nrow = 0;
+        for (int j = 0; j < 8; ++j) {
+            int r = 0;
+            while (r < sp.nrow && std::memcmp(sp.W[r], extrap + 8 * j, sizeof(double) * 8) != 0) ++r;
+            if (r == sp.nrow) {
+                for (int k = 0; k < 8; ++k) sp.W[r][k] = extrap[8 * j + k];
+                ++sp.nrow;
+            }
+            sp.row_of[j] = r;
+        }
         const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
         k_stress_element<<<unsigned(blocks), kThreads, 0, st>>>(sp);
         FEM_LAUNCH_CHECK("k_stress_element");
