@@ -395,12 +395,15 @@ struct StressDdParams {
     float2* rec;            // 8 * n_elem records of 6 float pairs
     float2 D0d, lam, mu;
     float2 dnr[8][8][3];
-    float2 W[8][8];
+    float2 W[8][8];  // the distinct rows of the caller's extrapolation table
+    int nrow;        // how many
+    int row_of[8];   // corner j -> its row of W
 };
 
 struct StressDdSmem {
     float2 dnr[8][8][3];
     float2 W[8][8];
+    float2 res[kEpc][8][6];  // extrapolated values of each distinct table row
     float2 x[kEpc][8][3];
     float2 u[kEpc][8][3];
     float2 sv[kEpc][8][kSvPad];
@@ -504,21 +507,24 @@ __global__ void __launch_bounds__(kThreads) k_stress_element_dd(const StressDdPa
         s.sv[el][g][5] = stp(dd_mul(mu, dd_add(H[0][2], H[2][0])));
     }
     __syncthreads();
+    // the table's distinct rows only, spread over the element's threads (as the FP64 kernel)
+    if (valid) {
+        const int nout = p.nrow * 6;
+        for (int o = t; o < nout; o += 8) {
+            const int r = o / 6, c = o - 6 * r;
+            dd_acc acc = acc_zero();
+#pragma unroll
+            for (int k = 0; k < 8; ++k) acc_fma(acc, ldp(s.W[r][k]), ldp(s.sv[el][k][c]));
+            s.res[el][r][c] = stp(acc_value(acc));
+        }
+    }
+    __syncthreads();
     if (!valid) return;
-    const int j = t;
+    const int j = t, r = p.row_of[j];
     const int64_t slot = p.ne_inv ? int64_t(__ldg(p.ne_inv + e * 8 + j)) : e * 8 + j;
     float2* o = p.rec + slot * 6;
-    dd_acc acc[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] = acc_zero();
-#pragma unroll 1
-    for (int k = 0; k < 8; ++k) {
-        const dd w = ldp(s.W[j][k]);
-#pragma unroll
-        for (int c = 0; c < 6; ++c) acc_fma(acc[c], w, ldp(s.sv[el][k][c]));
-    }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) o[c] = stp(acc_value(acc[c]));
+    for (int c = 0; c < 6; ++c) o[c] = s.res[el][r][c];
 }
 
 // Cyclic Jacobi on a symmetric 3x3 in double-float; returns the eigenvalues descending.
@@ -644,8 +650,20 @@ int launch_stress_dd(const fem_mesh* mesh, const fem_material* mat, const double
         for (int g = 0; g < 8; ++g)
             for (int a = 0; a < 8; ++a)
                 for (int d = 0; d < 3; ++d) split2(T.dnr[g][a][d], sp.dnr[g][a][d]);
-        for (int j = 0; j < 8; ++j)
-            for (int k = 0; k < 8; ++k) split2(extrap[8 * j + k], sp.W[j][k]);
+        // distinct rows of the table (exactly equal rows share one), split into float pairs
+        std::memset(sp.W, 0, sizeof(sp.W));
+        int first[8];  // the first corner of each distinct row
+        sp.nrow = 0;
+        for (int j = 0; j < 8; ++j) {
+            int r = 0;
+            while (r < sp.nrow && std::memcmp(extrap + 8 * first[r], extrap + 8 * j, sizeof(double) * 8) != 0) ++r;
+            if (r == sp.nrow) {
+                for (int k = 0; k < 8; ++k) split2(extrap[8 * j + k], sp.W[r][k]);
+                first[r] = j;
+                ++sp.nrow;
+            }
+            sp.row_of[j] = r;
+        }
         const int64_t blocks = (mesh->n_elem + kEpc - 1) / kEpc;
         k_stress_element_dd<<<unsigned(blocks), kThreads, 0, st>>>(sp);
         FEM_LAUNCH_CHECK("k_stress_element_dd");
