@@ -152,10 +152,11 @@ int fem_assemble_gather(const fem_mesh* mesh, const fem_assembly_out* out, const
 
 /* Assembly delivered to host memory: replaces the reference getters' "run the kernels, then
  * to_numpy()" (Get_MatrixKL / Get_MatrixM / Get_VectorF, FEM_model_csr.py:118-146).  The
- * mesh is assembled in n_parts parts of consecutive block rows; part q's rows are copied
- * from the device outputs in `out` to K_host / M_host / F_host (same layouts as out; NULL
- * skips one) on an internal copy stream while later parts still compute, so the copies
- * overlap the kernels.  The plan comes from fem_pipeline_plan.  Host buffers may be
+ * mesh is assembled in n_parts parts of consecutive block rows: element parts run on `stream`,
+ * the gathers on an internal high-priority stream (gather q after element part q, beside
+ * element part q + 1), and part q's rows are copied from the device outputs in `out` to
+ * K_host / M_host / F_host (same layouts as out; NULL skips one) on an internal copy stream
+ * while later parts still compute, so the copies overlap the kernels.  The plan comes from fem_pipeline_plan.  Host buffers may be
  * page-locked (copies asynchronous) or pageable (copies then finish before the call
  * returns).  `stream` is ordered after the last copy: synchronise it before reading the host
  * buffers.  Not capturable into a CUDA graph.  FEM_ALGO_FP64 without mesh->slot_map runs as
