@@ -437,10 +437,27 @@ __global__ void __launch_bounds__(256) k_gather(const GatherParams p) {
 // lane-per-slot path (same order).
 constexpr int kG64Warps = 4;
 constexpr int kG64Rows = 4;
-// 27 slots: every row of a structured hex mesh (3 x 3 x 3 neighbour nodes); the row
-// accumulators of a CTA then take 37 KB, so 6 CTAs (24 warps) fit on an SM instead of 5.
+// 27 slots: every row of a structured hex mesh (3 x 3 x 3 neighbour nodes).  A row's
+// accumulator holds 29 positions of 10 doubles (2,320 bytes; 16 rows per CTA take 36 KB, so 6
+// CTAs (24 warps) fit on an SM).  A row of 27 slots places slot s at kPos27(s): each element's 8
+// corners hit a 2 x 2 x 2 sub-cube of the 3 x 3 x 3 neighbourhood, and the table gives the 8
+// slots of every such sub-cube distinct positions mod 8, so the 16-byte accesses of a row's 8
+// lanes fall in 8 different bank groups (in slot order, slots 8 apart collided).  No placement
+// in 27 positions does that (the centre slot lies in all 8 sub-cubes, so its residue can hold
+// nothing else); the table uses 29.  Other rows keep position = slot.  Any one-to-one placement
+// gives the same sums; the table only removes bank conflicts.
 constexpr int kG64MaxL = 27;
-constexpr int kG64RowStride = kG64MaxL * kPairStride + 6;  // +6 doubles: rows start 8 banks apart
+constexpr int kG64Pos = 29;
+constexpr int kG64RowStride = kG64Pos * kPairStride;
+
+// Position of slot s (0..26) in a row of 27 slots: 5 bits per slot, 12 slots per word.  The
+// classes of equal position mod 8: {the 4 centres of the x edges}, 4 x {a face centre, the
+// edge centre and 2 corners that complete its exact cover of the 8 sub-cubes}, 2 x {a z face
+// centre, 2 edge centres}, {the centre}.
+__device__ __forceinline__ int pos27(int s) {
+    const unsigned long long w = s < 12 ? 0x048d9144ec575012ull : (s < 24 ? 0x0a99bc86964508e1ull : 0x671bull);
+    return int((w >> (5 * (s - 12 * (s / 12)))) & 31ull);
+}
 
 struct Gather64Params {
     int64_t row_begin, row_end;  // block rows [row_begin, row_end) of this launch
@@ -462,18 +479,7 @@ struct Gather64Params {
 
 struct Gather64Smem {
     double acc[kG64Warps][kG64Rows][kG64RowStride];
-    int cols[kG64Warps][kG64Rows][kG64MaxL];
 };
-
-__device__ __forceinline__ int find_slot64(const int* cols, int L, int node) {
-    int lo = 0, hi = L - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (cols[mid] < node) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
 
 // Lane-per-slot path for one row of any length (K and M; F is summed by the caller).
 __device__ void gather_row_long64(const Gather64Params& p, int64_t row, int lane) {
@@ -562,8 +568,13 @@ __global__ void __launch_bounds__(kG64Warps * 32, 6) k_gather64(const Gather64Pa
         return;
     }
 
-    int* cols = S.cols[w][r];
-    for (int l = b; l < kG64MaxL; l += 8) cols[l] = l < L ? __ldg(p.indices + rs + l) : INT_MAX;
+    // the row's diagonal slot (-1 if the node is not its own neighbour), found by the 8 lanes
+    int diag = -1;
+    for (int l = b; l < L; l += 8)
+        if (__ldg(p.indices + rs + l) == int(row)) diag = l;
+#pragma unroll
+    for (int off = 1; off < 8; off <<= 1) diag = max(diag, __shfl_xor_sync(full, diag, off));
+    const bool full27 = L == kG64MaxL;
     double* accr = S.acc[w][r];
 
     int maxcnt = cnt;
@@ -635,7 +646,7 @@ __global__ void __launch_bounds__(kG64Warps * 32, 6) k_gather64(const Gather64Pa
             if (bp < b && other == cur_slot) dup = true;
         }
         const unsigned bit = 1u << cur_slot;
-        double* a = accr + cur_slot * kPairStride;
+        double* a = accr + (full27 ? pos27(cur_slot) : cur_slot) * kPairStride;
         if (active && !dup) {
             if (touched & bit) {
 #pragma unroll
@@ -674,13 +685,13 @@ __global__ void __launch_bounds__(kG64Warps * 32, 6) k_gather64(const Gather64Pa
         const int LL = __shfl_sync(full, L, rr * 8);
         const unsigned tch = __shfl_sync(full, touched, rr * 8);
         const unsigned fixed_bits = p.fixed ? p.fixed[rw] : 0u;
-        const int* cc = S.cols[w][rr];
-        const int sd = LL > 0 ? find_slot64(cc, LL, int(rw)) : 0;
-        const bool has_diag = LL > 0 && cc[sd] == int(rw);
+        const int sd = __shfl_sync(full, diag, rr * 8);
+        const bool has_diag = sd >= 0;
+        const bool f27 = LL == kG64MaxL;
         const double* acc = S.acc[w][rr];
         auto value = [&](int s_, int q) -> double {
             if (!((tch >> s_) & 1u)) return 0.0;
-            double v = acc[s_ * kPairStride + q];
+            double v = acc[(f27 ? pos27(s_) : s_) * kPairStride + q];
             if (q < 9 && has_diag && s_ == sd && (q % 4 == 0) && ((fixed_bits >> (q / 4)) & 1u)) v = 1e20;
             return v;
         };
