@@ -73,7 +73,9 @@ struct ElemParams {
 };
 
 struct ElemSmem {
-    double dnr[8][8][3];
+    double dnr[8][kRPad];       // dN_a/dxi_i at Gauss point g at [g][3a+i]; padded row: the 8 rows
+                                // start in 8 different bank pairs (a 24-double row put every
+                                // even g in one bank and every odd g in another)
     double x[kEpc][8][3];       // corner coordinates; later the first mass contraction (D1)
     double xl[kEpc][8][3];      // corner coordinates relative to corner 0; later D2
     double cf[kEpc][8][3];      // trilinear coefficients c_k of the element map (c_0 unused)
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
     const int64_t e = p.e_begin + int64_t(blockIdx.x) * kEpc + el;
     const bool valid = e < p.e_end;
 
-    for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) (&s.dnr[0][0][0])[k] = (&p.tab.dnr[0][0][0])[k];
+    for (int k = tid; k < 8 * 8 * 3; k += kElemThreads) s.dnr[k / 24][k % 24] = (&p.tab.dnr[0][0][0])[k];
     if (valid) {
         const int* cn = reinterpret_cast<const int*>(p.conn4) + 8 * e;
         const int node = __ldg(cn + t);
@@ -182,7 +184,8 @@ __global__ void __launch_bounds__(kElemThreads, 3) k_hex8_element(const ElemPara
         for (int a = 0; a < 8; ++a)
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                const double r = s.dnr[g][a][0] * A[0][i] + s.dnr[g][a][1] * A[1][i] + s.dnr[g][a][2] * A[2][i];
+                const double r =
+                    s.dnr[g][3 * a] * A[0][i] + s.dnr[g][3 * a + 1] * A[1][i] + s.dnr[g][3 * a + 2] * A[2][i];
                 s.R[el][g][3 * a + i] = r;
                 s.Rs[el][g][3 * a + i] = r * inv;
             }
